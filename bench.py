@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the PBF substep pipeline (particle-iterations/s).
+
+Workload: the 1,048,576-particle dam break (position-based-fluids_gb300/
+scenarios/dam_break_1m.par: a 128x64x128 block at spacing 0.05 with seeded
+jitter in a 12.8 x 6.4 x 6.4 box, h = 0.1, 4 solver iterations).  One bench
+step is one 1/60 s frame = 2 substeps of Simulation::Step.
+
+  value  : particle-iterations/s = N * iterations * substeps / time, with the
+           state resident in HBM; CUDA events on the library's stream around
+           K frames (after W warm-up frames), max over ranks.
+  e2e    : the same metric through the C-ABI with host buffers: every frame
+           copies positions + velocities in from pinned host memory, steps,
+           and copies them back out (wall clock).
+  roofline: the dominant kernel's algorithmic bytes per launch over its
+           average launch time (CUDA events between stages on the library's
+           stream, in a separate pass of the same frames), against the
+           measured HBM copy bandwidth.
+
+--impl reference times the CPU restatement of the reference's pipeline
+(OpenMP over all host cores) on the same scene instead.
+Multi-GPU (torchrun): every rank advances its own replica of the scene;
+value sums the particles of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+PKG = REPO / "position-based-fluids_gb300"
+for _p in (str(REPO), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "particle-iterations/s at 1M particles (plain PBF substep pipeline)"
+UNIT = "particle-iterations/s"
+SCENE = "dam_break_1m"
+FALLBACK_HBM_GBS = 6800.0
+
+# Per-particle algorithmic bytes of one launch of each stage (compulsory
+# reads and writes of the particle records, the keys and the neighbour list;
+# neighbour records gathered through the caches are not counted).  `nl` / `nd`
+# are the mean neighbour-list lengths of the density pass / the other passes.
+STAGE_BYTES = {
+    "predictPositions": lambda nl, nd: 72.0,
+    "sortParticles": lambda nl, nd: 68.0,
+    "updateCells": lambda nl, nd: 12.0,
+    "buildFriendsList": lambda nl, nd: 20.0 + 4.0 * nl,
+    "resetPartList": lambda nl, nd: 12.0,
+    "computeScaling": lambda nl, nd: 40.0 + 4.0 * nl,
+    "computeDelta": lambda nl, nd: 40.0 + 4.0 * nd,
+    "updateVelocities": lambda nl, nd: 80.0,
+    "applyViscosity": lambda nl, nd: 68.0 + 4.0 * nd,
+    "applyVorticity": lambda nl, nd: 68.0 + 4.0 * nd,
+}
+
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def measured_peaks() -> tuple[float, str]:
+    path = REPO / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(path.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, device_index: int):
+        self.device = device_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={CLOCK_FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[0] == str(self.device):
+                    rows.append(f)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clocks not sampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(params, pos, vel, seconds: float) -> dict:
+    """The oracle (CPU restatement, OpenMP) on a bounded sample of the scene."""
+    from oracle import oracle
+    threads = oracle.max_threads()
+    n, iters = int(params.particleCount), int(params.simIterations)
+    done, t0 = 0, time.perf_counter()
+    p, v = pos, vel
+    while True:
+        p, v, _ = oracle.step(params, p, v, 1, threads=threads)
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return {"value": n * iters * done / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done} substep(s) of the {n}-particle scene from its initial state, {el:.1f} s"}
+
+
+def reference_arm(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import pbf
+    from oracle import oracle
+    params, pos, vel = pbf.make_scene(args.scene)
+    n, iters = int(params.particleCount), int(params.simIterations)
+    threads = oracle.max_threads()
+    p, v = pos, vel
+    for _ in range(min(args.warmup, 1)):
+        p, v, _ = oracle.step(params, p, v, 1, threads=threads)
+    done, t0 = 0, time.perf_counter()
+    budget = args.cpu_budget
+    while done < args.steps:
+        p, v, _ = oracle.step(params, p, v, 1, threads=threads)
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    value = n * iters * done / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": 1000.0 * el / done,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{args.scene}: {n} particles, {iters} iterations; one step = one substep",
+                   "threads": threads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{done} substep(s) from the initial state (time budget {budget:.0f} s)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def gpu_arm(args) -> None:
+    import numpy as np
+    import torch
+    import pbf
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    params, pos, vel = pbf.make_scene(args.scene)
+    n, iters, sub = int(params.particleCount), int(params.simIterations), int(params.subSteps)
+    sim = pbf.Simulation.create(params, pos, vel, device=local)
+    stream = torch.cuda.ExternalStream(sim.stream(), device=torch.device("cuda", local))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        sim.step_async(sub)
+    sim.synchronize()
+
+    # ---- timed region: K frames, state resident in HBM ----
+    barrier()
+    launches0 = sim.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.step_async(sub)
+        ev1.record(stream)
+        ev1.synchronize()
+    sim.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    launches = sim.launch_count() - launches0
+    t = torch.tensor([ms], device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    value = world * n * iters * sub * args.steps / (ms / 1000.0)
+
+    # ---- end to end through the C-ABI with pinned host buffers ----
+    hpos = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+    hvel = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+    sim.read_state_into(hpos.data_ptr(), hvel.data_ptr())
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    for _ in range(3):
+        sim.write_state_from(hpos.data_ptr(), hvel.data_ptr())
+        sim.Step(sub)
+        sim.read_state_into(hpos.data_ptr(), hvel.data_ptr())
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.write_state_from(hpos.data_ptr(), hvel.data_ptr())
+        sim.Step(sub)
+        sim.read_state_into(hpos.data_ptr(), hvel.data_ptr())
+    e2e_s = time.perf_counter() - t0
+    t = torch.tensor([e2e_s], device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_value = world * n * iters * sub * e2e_steps / float(t.item())
+
+    # ---- per-stage device times (eager launches, events between stages) ----
+    counts, _ = sim.read_friends(slots=1)
+    nl, nd = float(counts[:, 0].mean()), float(counts[:, 1].mean())
+    sim.enable_stage_timing(True)
+    frames = max(1, min(args.steps, 20))
+    totals: dict[str, float] = {}
+    for _ in range(frames):
+        sim.Step(sub)
+        for k, v in sim.stage_timings().items():
+            totals[k] = totals.get(k, 0.0) + v
+    sim.enable_stage_timing(False)
+    per_frame_launches = {"computeScaling": iters * sub, "computeDelta": iters * sub}
+    stage_ms = {k: v / frames for k, v in totals.items()}
+    dominant = max((k for k in stage_ms if k in STAGE_BYTES), key=lambda k: stage_ms[k])
+    launches_per_frame = per_frame_launches.get(dominant, sub)
+    launch_ms = stage_ms[dominant] / launches_per_frame
+    algo_bytes = STAGE_BYTES[dominant](nl, nd) * n
+    peak, peak_kind = measured_peaks()
+    achieved = algo_bytes / (launch_ms / 1000.0) / 1e9
+    frame_ms = ms / args.steps
+    bytes_sub = (444.0 + 56.0 * iters) * n  # whole-substep compulsory bytes, P = 3 sort passes
+    pipeline_gbs = bytes_sub * sub / (frame_ms / 1000.0) / 1e9
+
+    if rank != 0:
+        sim.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    base = None
+    if world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(params, pos, vel, args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{args.scene}: {n} particles (128x64x128 block, spacing 0.05, seeded jitter) "
+                               f"in a 12.8x6.4x6.4 box; {iters} iterations x {sub} substeps per step (frame)",
+                   "particles": n, "iterations": iters, "substeps_per_step": sub,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "working set larger than L2 (no flush)", "mode": "reference-exact FP32 (no FMA contraction)",
+                   "cuda_graph": True},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
+                "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": launch_ms},
+        "pipeline_roofline": {"bytes_per_particle_substep": 444.0 + 56.0 * iters, "achieved": pipeline_gbs,
+                              "frac": pipeline_gbs / peak},
+        "stage_ms_per_step": {k: round(v, 4) for k, v in sorted(stage_ms.items(), key=lambda kv: -kv[1])},
+        "neighbours": {"density_pass": nl, "other_passes": nd},
+        "clocks": clocks.summary(),
+    }
+    if base is not None:
+        line["cpu_baseline"] = base
+    print(json.dumps(line), flush=True)
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--scene", default=SCENE)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-budget", type=float, default=150.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "gb300":
+        args.warmup = max(3, args.warmup)  # at least 3 untimed frames
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

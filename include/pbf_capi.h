@@ -1,0 +1,201 @@
+/*
+ * pbf_capi.h — C-ABI of the GB300 PBF substep pipeline.
+ *
+ * The reference drives this path through the C++ class `Simulation`
+ * (src/Simulation.hpp:28-151) and the global `Parameters Params` with its
+ * loader `LoadParameters` (src/ParamUtils.hpp, src/ParamUtils.cpp:19-100).
+ * Every entry point below replaces one of those members; the citation on each
+ * names the member it stands in for.
+ *
+ * Conventions
+ *   - Every function returns an int status: PBF_OK (0) or a negative PBF_ERR_*.
+ *     `pbf_last_error(ctx)` returns the message of the last failure on that
+ *     context (ctx == NULL: the last failure of a call that had no context).
+ *     No C++ exception crosses this boundary.
+ *   - Particle arrays are float4 records (x, y, z, w) stored as 4 consecutive
+ *     floats, `particleCount` records long, in host memory unless a name says
+ *     `device`.
+ *   - The handle is opaque; the library owns all device memory of a context.
+ *   - One CUDA stream per context; calls on one context are not re-entrant,
+ *     contexts on different host threads are independent.
+ */
+#ifndef PBF_CAPI_H
+#define PBF_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "pbf_params.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBF_OK                 0
+#define PBF_ERR_INVALID       -1   /* bad argument or parameter value        */
+#define PBF_ERR_CUDA          -2   /* a CUDA runtime call failed             */
+#define PBF_ERR_STATE         -3   /* call out of order (e.g. step before init) */
+#define PBF_ERR_UNSUPPORTED   -4   /* feature of the reference not built here */
+#define PBF_ERR_DEVICE_FLAG   -5   /* a kernel raised its error word          */
+#define PBF_ERR_NO_DEVICE     -6   /* no usable CUDA device                   */
+
+typedef struct pbf_ctx pbf_ctx;
+
+/* ---------------------------------------------------------------- params -- */
+
+/* Zero-filled parameters with the loader's computed fields applied
+   (h_2 = h*h, friendsCircles = 5, particlesPerCircle = 50).
+   Replaces the zero-initialised global `Parameters Params`
+   (src/ParamUtils.cpp:19). */
+int pbf_default_parameters(PbfParameters* out);
+
+/* Parse `.par` text into *inout, updating only the keys present, then apply
+   the computed fields.  Same grammar and error behaviour as
+   `LoadParameters(string)` (src/ParamUtils.cpp:24-100): one `key value` per
+   line, `#` starts a comment, keys case-insensitive, unknown keys reported on
+   stderr and ignored, and a final line with no trailing newline is dropped
+   with "Error parsing parameters file".  Extra keys accepted here:
+   gravityx / gravityy / gravityz (any of them enables the gravity vector) and
+   boxclamp.  Returns the number of unknown keys through *unknown (may be NULL). */
+int pbf_load_parameters(const char* text, PbfParameters* inout, int* unknown);
+
+/* -------------------------------------------------------------- lifetime -- */
+
+/* Create a context on CUDA device `device`.
+   Replaces Simulation::Simulation(const cl::Context&, const cl::Device&)
+   (src/Simulation.cpp:56-63): the in-order profiling queue becomes one CUDA
+   stream. */
+int pbf_create(const PbfParameters* params, int device, pbf_ctx** out);
+
+/* Release every device allocation of the context.
+   Replaces Simulation::~Simulation (src/Simulation.cpp:65-69). */
+int pbf_destroy(pbf_ctx* ctx);
+
+/* Message of the last failure (never NULL). */
+const char* pbf_last_error(const pbf_ctx* ctx);
+
+/* ------------------------------------------------------ init (reference) -- */
+
+/* Allocate the particle buffers for params.particleCount particles and load
+   the initial state.  init_pos == NULL: the reference's CreateParticles
+   lattice (src/Simulation.cpp:71-101); init_vel == NULL: zero velocities.
+   Replaces Simulation::InitBuffers (src/Simulation.cpp:206-244). */
+int pbf_init_buffers(pbf_ctx* ctx, const float* init_pos, const float* init_vel);
+
+/* Allocate the cell table (gridBufSize entries, every entry 0xFFFFFFFF) and
+   the neighbour ("friends") list storage.
+   Replaces Simulation::InitCells (src/Simulation.cpp:246-255). */
+int pbf_init_cells(pbf_ctx* ctx);
+
+/* Load the force-plane mask image.  Only mask == NULL (an all-zero mask, for
+   which BouncePointQuad is the identity: compute_delta.cl:33-38) is
+   supported; a non-NULL mask returns PBF_ERR_UNSUPPORTED.
+   Replaces Simulation::LoadForceMasks (src/Simulation.cpp:257-281). */
+int pbf_load_force_masks(pbf_ctx* ctx, const uint32_t* mask, int width, int height);
+
+/* Validate the parameters against the allocated buffers and prepare the
+   launch plan (sort passes, grid shapes).  Returns PBF_ERR_INVALID where the
+   reference's InitKernels would have failed to build.
+   Replaces bool Simulation::InitKernels (src/Simulation.cpp:129-204). */
+int pbf_init_kernels(pbf_ctx* ctx);
+
+/* Replace the parameters of an initialised context (same particleCount and
+   gridBufSize).  Stands in for the reference's reload of `Params` followed by
+   the re-upload at src/Simulation.cpp:243. */
+int pbf_set_params(pbf_ctx* ctx, const PbfParameters* params);
+
+/* Simulation::bPauseSim (src/Simulation.hpp:146): when set, a step adds no
+   gravity and skips the sort (src/Simulation.cpp:563-567). */
+int pbf_set_pause(pbf_ctx* ctx, int paused);
+
+/* ------------------------------------------------------------------ step -- */
+
+/* Run Simulation::Step() (src/Simulation.cpp:554-621) `substeps` times and
+   wait for the device.  Each substep uses the full params.timeStep, as the
+   reference's frame loop does (src/Runner.cpp:124-130). */
+int pbf_step(pbf_ctx* ctx, int substeps);
+
+/* As pbf_step, but only enqueues the work on the context's stream. */
+int pbf_step_async(pbf_ctx* ctx, int substeps);
+
+/* Wait for all work enqueued on the context's stream; reports a kernel error
+   word raised since the last check as PBF_ERR_DEVICE_FLAG. */
+int pbf_synchronize(pbf_ctx* ctx);
+
+/* ----------------------------------------------------------------- state -- */
+
+/* Copy the current state to host memory (any pointer may be NULL):
+   positions (w = |v|, update_velocities.cl:14), velocities, and predicted
+   positions (w = density after a step, pack_data.cl with the density source).
+   Replaces reading the GL-shared position buffers the renderer draws. */
+int pbf_read_state(pbf_ctx* ctx, float* pos, float* vel, float* pred);
+
+/* Overwrite positions and velocities from host memory (either may be NULL). */
+int pbf_write_state(pbf_ctx* ctx, const float* pos, const float* vel);
+
+/* Device address of the current positions (float4 x particleCount), valid
+   until the next step.  Headless replacement of the GL buffer IDs
+   mSharedPingBufferID / mSharedPongBufferID (src/Simulation.hpp:130-135). */
+int pbf_device_positions(pbf_ctx* ctx, void** dptr);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+   work against it. */
+int pbf_get_stream(pbf_ctx* ctx, void** stream);
+
+/* ----------------------------------------------------------- parity hooks -- */
+
+/* From the predicted positions `pred` (host), run the key / sort / cell-table
+   stages alone and copy out
+     keys  : IntCeil(N, 2048) sorted keys, padding entries 2147483646
+             (radixsort.cl:1-20, Simulation.cpp:223),
+     perm  : the same length, the sort permutation,
+     cells : 2 * gridBufSize words, start / inclusive end per hash,
+             0xFFFFFFFF for empty hashes (update_cells.cl:1-26).
+   Any output may be NULL.  The context's particle state is not changed. */
+int pbf_sort_state(pbf_ctx* ctx, const float* pred,
+                   uint32_t* keys, uint32_t* perm, uint32_t* cells);
+
+/* Neighbour ("friends") list of the last substep, as used by the solver:
+   counts[2*i+0] = entries used by computeScaling (circles kept while
+   processed/total <= 0.6, compute_scaling.cl:47-54), counts[2*i+1] = entries
+   used by computeDelta / applyViscosity / applyVorticity (<= 0.5,
+   compute_delta.cl:97-104); list[s * N + i] = s-th neighbour of particle i in
+   circle-major order (build_friends_list.cl:74-94).  `list_slots` is the
+   number of slots the caller's list buffer holds per particle; entries beyond
+   it are not copied.  Either pointer may be NULL. */
+int pbf_read_friends(pbf_ctx* ctx, uint32_t* counts, uint32_t* list, int list_slots);
+
+/* ------------------------------------------------------------ diagnostics -- */
+
+/* Per-stage device times of the last pbf_step with stage timing enabled, in
+   milliseconds, under the reference tracker names (OCLPerfMon usage in
+   src/Simulation.cpp:315-535).  names receives a '\n'-separated list. */
+int pbf_enable_stage_timing(pbf_ctx* ctx, int enable);
+int pbf_stage_timings(pbf_ctx* ctx, float* ms, int capacity, int* count,
+                      char* names, size_t names_len);
+
+/* Number of kernels this context has launched so far (graph nodes counted
+   one by one). */
+int pbf_launch_count(pbf_ctx* ctx, uint64_t* count);
+
+/* Use (1) or stop using (0) a captured CUDA graph for each substep. */
+int pbf_use_graph(pbf_ctx* ctx, int enable);
+
+/* ------------------------------------------------------------- scenarios -- */
+
+/* The reference's initial lattice (Simulation::CreateParticles,
+   src/Simulation.cpp:71-101) for params->particleCount particles. */
+int pbf_reference_lattice(const PbfParameters* params, float* pos);
+
+/* A jittered block lattice: particle i = ix + nx*(iy + ny*iz) sits at
+   origin + (ix, iy, iz) * spacing + u, u uniform in [-jitter, jitter) per
+   component from std::mt19937_64(seed); w = 0.  Computed in double, rounded
+   once to float. */
+int pbf_scene_block(int nx, int ny, int nz, float spacing,
+                    float ox, float oy, float oz,
+                    float jitter, uint64_t seed, float* pos);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBF_CAPI_H */

@@ -1,0 +1,81 @@
+/*
+ * pbf_params.h — scenario parameters of the PBF substep pipeline.
+ *
+ * PbfParameters keeps the field order, types and meaning of the reference's
+ * `struct Parameters` (src/Parameters.hpp:5-56; the kernel-side copy is
+ * assets/kernels/parameters.hpp) so that a caller holding a filled
+ * `Parameters` can hand its bytes over unchanged: the prefix up to and
+ * including `EnableCachedBuffers` is layout-identical.  New fields are only
+ * appended after it.
+ *
+ * Reference semantics kept verbatim, including the misspelled names
+ * (`garvity`, `surfaceTenstionK`, `surfaceTenstionDist`):
+ *   - mass is implicitly 1;
+ *   - `garvity` is a scalar applied along -y (predict_positions.cl:13) unless
+ *     the appended gravity vector is enabled;
+ *   - `friendsCircles` / `particlesPerCircle` are forced to 5 / 50 and
+ *     `h_2 = h*h` by the loader (src/ParamUtils.cpp:97-99);
+ *   - xMin..zMax are never read by the reference kernels; here they bound the
+ *     box clamp when `boxClamp` is set.
+ */
+#ifndef PBF_PARAMS_H
+#define PBF_PARAMS_H
+
+#include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct PbfParameters {
+    /* ---- prefix identical to src/Parameters.hpp:5-56 ---- */
+    int          resetSimOnChange;
+    unsigned int particleCount;
+    float        xMin, xMax, yMin, yMax, zMin, zMax;
+    float        waveGenAmp, waveGenFreq, waveGenDuty;
+    float        timeStep;
+    unsigned int simIterations;
+    unsigned int subSteps;
+    float        h;
+    float        restDensity;
+    float        epsilon;
+    float        garvity;
+    float        vorticityFactor;
+    float        viscosityFactor;
+    float        surfaceTenstionK;
+    float        surfaceTenstionDist;
+    unsigned int friendsCircles;
+    unsigned int particlesPerCircle;
+    unsigned int gridBufSize;
+    float        setupSpacing;
+    unsigned int segmentSize;
+    unsigned int sortIterations;
+    float        particleRenderSize;
+    float        h_2;
+    bool         EnableCachedBuffers;
+    /* ---- appended fields (not in the reference) ---- */
+    /* 0: gravity is (0, -garvity, 0) exactly as the reference;
+       1: gravity is (gravityX, gravityY, gravityZ). */
+    int          gravityVectorEnable;
+    float        gravityX, gravityY, gravityZ;
+    /* 1: clamp pred + delta_p to [xMin,xMax]x[yMin,yMax]x[zMin,zMax] inside
+       the delta-p stage, after the position update is formed and before the
+       delta is taken.  0: no clamp (the reference's behaviour). */
+    int          boxClamp;
+} PbfParameters;
+
+/* Largest friend-circle configuration the kernels accept. */
+#define PBF_MAX_CIRCLES            8
+#define PBF_MAX_PER_CIRCLE         64
+/* Largest particle count: the reference's sort limit _N = 1<<23
+   (assets/kernels/hesp.hpp:77) times 8. */
+#define PBF_MAX_PARTICLES          (1u << 26)
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBF_PARAMS_H */

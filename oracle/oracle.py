@@ -1,0 +1,161 @@
+"""ctypes binding of the test oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.  ``step`` runs the FP32 restatement of Simulation::Step,
+``step_f64`` the FP64 one, ``sort`` the key / sort / cell-table stages, and
+``ref_step`` / ``ref_sort`` the reference's own kernels compiled through the
+OpenCL-C shim (available where oracle/_ref was built).
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_float, c_double, c_int, c_uint32, c_void_p
+
+import numpy as np
+
+from . import build as _build  # noqa: F401  (package-relative when imported as oracle.oracle)
+
+
+class OracleDebug(ctypes.Structure):
+    _fields_ = [
+        ("keys", c_void_p), ("perm", c_void_p), ("cells", c_void_p), ("counts", c_void_p),
+        ("list", c_void_p), ("list_slots", c_int), ("density", c_void_p), ("lambda_", c_void_p),
+        ("omega", c_void_p),
+    ]
+
+
+_lib = None
+_ref = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        l = ctypes.CDLL(str(path))
+        l.oracle_step_f32.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_int,
+                                      POINTER(OracleDebug)]
+        l.oracle_step_f64.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int]
+        l.oracle_sort_f32.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]
+        l.oracle_constants.argtypes = [c_void_p, POINTER(c_float), POINTER(c_float), POINTER(c_float)]
+        l.oracle_grid_hash.argtypes = [c_int, c_int, c_int, c_uint32]
+        l.oracle_grid_hash.restype = c_uint32
+        for f in (l.oracle_step_f32, l.oracle_step_f64, l.oracle_sort_f32, l.oracle_constants, l.oracle_max_threads):
+            f.restype = c_int
+        _lib = l
+    return _lib
+
+
+def ref_available() -> bool:
+    return _build.REF_LIB.exists() or _build.REF_TU.exists() or (_build.REFERENCE / "assets").is_dir()
+
+
+def ref() -> ctypes.CDLL:
+    global _ref
+    if _ref is None:
+        path = _build.build_ref()
+        if path is None:
+            raise FileNotFoundError("the reference kernels are not available (oracle/_ref)")
+        l = ctypes.CDLL(str(path))
+        l.ref_step_f32.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]
+        l.ref_sort_f32.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]
+        l.ref_step_f32.restype = c_int
+        l.ref_sort_f32.restype = c_int
+        _ref = l
+    return _ref
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def n_keys(n: int) -> int:
+    return (n + 2047) // 2048 * 2048
+
+
+def step(params, pos, vel, substeps=1, paused=False, keys_state=None, threads=0, debug=False):
+    """FP32 oracle.  Returns (pos, vel, pred[, debug dict])."""
+    n = int(params.particleCount)
+    pos = np.array(pos, np.float32, copy=True).reshape(n, 4)
+    vel = np.array(vel, np.float32, copy=True).reshape(n, 4)
+    pred = np.zeros((n, 4), np.float32)
+    dbg = None
+    out = {}
+    if debug:
+        slots = int(params.friendsCircles * params.particlesPerCircle)
+        out = dict(keys=np.zeros(n_keys(n), np.uint32), perm=np.zeros(n_keys(n), np.uint32),
+                   cells=np.zeros(2 * params.gridBufSize, np.uint32), counts=np.zeros((n, 2), np.uint32),
+                   list=np.zeros((slots, n), np.uint32), density=np.zeros(n, np.float32),
+                   lambda_=np.zeros(n, np.float32), omega=np.zeros((n, 4), np.float32))
+        dbg = OracleDebug(_ptr(out["keys"]), _ptr(out["perm"]), _ptr(out["cells"]), _ptr(out["counts"]),
+                          _ptr(out["list"]), slots, _ptr(out["density"]), _ptr(out["lambda_"]), _ptr(out["omega"]))
+    rc = lib().oracle_step_f32(ctypes.byref(params), n, _ptr(pos), _ptr(vel), _ptr(pred), substeps, int(paused),
+                               _ptr(keys_state), threads, ctypes.byref(dbg) if dbg is not None else None)
+    if rc != 0:
+        raise ValueError(f"oracle_step_f32 rejected the parameters ({rc})")
+    return (pos, vel, pred, out) if debug else (pos, vel, pred)
+
+
+def step_f64(params, pos, vel, substeps=1, threads=0):
+    n = int(params.particleCount)
+    pos = np.array(pos, np.float64, copy=True).reshape(n, 4)
+    vel = np.array(vel, np.float64, copy=True).reshape(n, 4)
+    pred = np.zeros((n, 4), np.float64)
+    rc = lib().oracle_step_f64(ctypes.byref(params), n, _ptr(pos), _ptr(vel), _ptr(pred), substeps, threads)
+    if rc != 0:
+        raise ValueError(f"oracle_step_f64 rejected the parameters ({rc})")
+    return pos, vel, pred
+
+
+def sort(params, pred):
+    n = int(params.particleCount)
+    pred = np.ascontiguousarray(pred, np.float32).reshape(n, 4)
+    keys = np.zeros(n_keys(n), np.uint32)
+    perm = np.zeros(n_keys(n), np.uint32)
+    cells = np.zeros(2 * params.gridBufSize, np.uint32)
+    rc = lib().oracle_sort_f32(ctypes.byref(params), n, _ptr(pred), _ptr(keys), _ptr(perm), _ptr(cells))
+    if rc != 0:
+        raise ValueError(f"oracle_sort_f32 rejected the parameters ({rc})")
+    return keys, perm, cells
+
+
+def constants(params):
+    a, b, c = c_float(), c_float(), c_float()
+    lib().oracle_constants(ctypes.byref(params), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    return a.value, b.value, c.value
+
+
+def grid_hash(x, y, z, grid):
+    return int(lib().oracle_grid_hash(x, y, z, grid))
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
+
+
+def ref_step(params, pos, vel, substeps=1):
+    """The reference's kernels through the shim.  Returns (pos, vel, pred, keys, perm, cells)."""
+    n = int(params.particleCount)
+    pos = np.array(pos, np.float32, copy=True).reshape(n, 4)
+    vel = np.array(vel, np.float32, copy=True).reshape(n, 4)
+    pred = np.zeros((n, 4), np.float32)
+    keys = np.zeros(n_keys(n), np.uint32)
+    perm = np.zeros(n_keys(n), np.uint32)
+    cells = np.zeros(2 * params.gridBufSize, np.uint32)
+    rc = ref().ref_step_f32(ctypes.byref(params), n, _ptr(pos), _ptr(vel), _ptr(pred), substeps, _ptr(keys),
+                            _ptr(perm), _ptr(cells))
+    if rc != 0:
+        raise ValueError(f"ref_step_f32 rejected the input ({rc})")
+    return pos, vel, pred, keys, perm, cells
+
+
+def ref_sort(params, pred):
+    n = int(params.particleCount)
+    pred = np.ascontiguousarray(pred, np.float32).reshape(n, 4)
+    keys = np.zeros(n_keys(n), np.uint32)
+    perm = np.zeros(n_keys(n), np.uint32)
+    cells = np.zeros(2 * params.gridBufSize, np.uint32)
+    rc = ref().ref_sort_f32(ctypes.byref(params), n, _ptr(pred), _ptr(keys), _ptr(perm), _ptr(cells))
+    if rc != 0:
+        raise ValueError(f"ref_sort_f32 rejected the input ({rc})")
+    return keys, perm, cells

@@ -1,0 +1,106 @@
+"""Build recipe for libpbf_gb300.so (the CUDA kernels plus the C-ABI).
+
+Compiles every translation unit of ``csrc/`` for sm_103a in parallel and links
+the shared library in-tree, next to this file.  Flags that matter for the
+arithmetic contract:
+
+* ``--fmad=false`` on the kernel translation units: no multiply-add
+  contraction, so each float operation is rounded on its own;
+* IEEE division and square root (nvcc's defaults; no ``--use_fast_math``);
+* ``-ffp-contract=off`` for all host code, so the constants formed on the
+  host are the same on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+REPO = PKG.parent
+CSRC = PKG / "csrc"
+OBJ = PKG / "_build"
+LIB = PKG / "libpbf_gb300.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+INCLUDES = ["-I", str(REPO / "include"), "-I", str(CSRC)]
+HOST_FLAGS = ["-fPIC", "-ffp-contract=off", "-fno-fast-math"]
+
+# translation unit -> extra nvcc flags
+CUDA_UNITS = {
+    "pbf_kernels.cu": ["--fmad=false"],
+    "pbf_sort.cu": [],
+    "pbf_capi.cu": ["--fmad=false"],
+}
+CXX_UNITS = ["params.cpp"]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return cand
+
+
+def _cuda_include() -> str:
+    nvcc = Path(_nvcc()).resolve()
+    return str(nvcc.parent.parent / "include")
+
+
+def _run(cmd: list[str]) -> tuple[int, str]:
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    return proc.returncode, proc.stdout + proc.stderr
+
+
+def _headers() -> list[Path]:
+    return sorted(CSRC.glob("*.h")) + sorted((REPO / "include").glob("*.h"))
+
+
+def _stale(obj: Path, src: Path) -> bool:
+    if not obj.exists():
+        return True
+    t = obj.stat().st_mtime
+    return any(p.stat().st_mtime > t for p in [src, *_headers(), Path(__file__)])
+
+
+def compile_commands() -> list[tuple[Path, Path, list[str]]]:
+    jobs = []
+    for unit, extra in CUDA_UNITS.items():
+        src, obj = CSRC / unit, OBJ / (unit + ".o")
+        cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", *extra, *INCLUDES,
+               "-Xcompiler", ",".join(HOST_FLAGS), "-c", str(src), "-o", str(obj)]
+        jobs.append((src, obj, cmd))
+    for unit in CXX_UNITS:
+        src, obj = CSRC / unit, OBJ / (unit + ".o")
+        cmd = ["g++", "-O2", "-std=c++17", *HOST_FLAGS, *INCLUDES, "-I", _cuda_include(),
+               "-c", str(src), "-o", str(obj)]
+        jobs.append((src, obj, cmd))
+    return jobs
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    OBJ.mkdir(exist_ok=True)
+    jobs = [j for j in compile_commands() if force or _stale(j[1], j[0])]
+    if jobs:
+        with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
+            results = list(ex.map(lambda j: _run(j[2]), jobs))
+        for (src, _, cmd), (rc, out) in zip(jobs, results):
+            if verbose and out:
+                sys.stderr.write(out)
+            if rc != 0:
+                sys.stderr.write(out)
+                raise RuntimeError(f"compile failed: {src.name}\n{' '.join(cmd)}")
+    objs = [str(o) for _, o, _ in compile_commands()]
+    if force or jobs or not LIB.exists():
+        tmp = LIB.with_suffix(".so.tmp")
+        rc, out = _run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart"])
+        if rc != 0:
+            sys.stderr.write(out)
+            raise RuntimeError("link failed")
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

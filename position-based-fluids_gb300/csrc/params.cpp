@@ -1,0 +1,144 @@
+// params.cpp — scenario parameters: the `.par` loader and the initial-state
+// generators.  Host code only; compiled with -ffp-contract=off so that the
+// generated positions are bit-identical on every host.
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstring>
+#include <iostream>
+#include <random>
+#include <sstream>
+#include <string>
+
+#include "pbf_capi.h"
+#include "pbf_internal.h"
+
+namespace {
+
+// The loader's computed fields (src/ParamUtils.cpp:97-99).
+void apply_computed_fields(PbfParameters* p) {
+    p->h_2 = p->h * p->h;
+    p->friendsCircles = 5;
+    p->particlesPerCircle = 50;
+}
+
+}  // namespace
+
+extern "C" int pbf_default_parameters(PbfParameters* out) {
+    if (!out) return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_default_parameters: out is NULL");
+    std::memset(out, 0, sizeof(*out));
+    apply_computed_fields(out);
+    return PBF_OK;
+}
+
+// Same grammar and error behaviour as LoadParameters (src/ParamUtils.cpp:24-100).
+extern "C" int pbf_load_parameters(const char* text, PbfParameters* p, int* unknown) {
+    if (!text || !p) return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_load_parameters: NULL argument");
+    int nUnknown = 0;
+    std::istringstream in{std::string(text)};
+    std::string line, key;
+    while (std::getline(in, line)) {
+        // A line read up to end-of-input without a newline leaves the stream
+        // not good(); the reference reports it and stops (ParamUtils.cpp:34-38).
+        if (!in.good()) {
+            std::cerr << "Error parsing parameters file" << std::endl;
+            break;
+        }
+        line.erase(std::find(line.begin(), line.end(), '#'), line.end());
+        if (line.empty()) continue;
+        std::transform(line.begin(), line.end(), line.begin(), [](unsigned char c) { return (char)std::tolower(c); });
+        std::istringstream fields(line);
+        if (!(fields >> key)) {
+            std::cerr << "Unable to read parameter" << std::endl;
+            continue;
+        }
+        if (key == "resetsimonchange") fields >> p->resetSimOnChange;
+        else if (key == "particlecount") fields >> p->particleCount;
+        else if (key == "xmin") fields >> p->xMin;
+        else if (key == "xmax") fields >> p->xMax;
+        else if (key == "ymin") fields >> p->yMin;
+        else if (key == "ymax") fields >> p->yMax;
+        else if (key == "zmin") fields >> p->zMin;
+        else if (key == "zmax") fields >> p->zMax;
+        else if (key == "wavegenamp") fields >> p->waveGenAmp;
+        else if (key == "wavegenfreq") fields >> p->waveGenFreq;
+        else if (key == "wavegenduty") fields >> p->waveGenDuty;
+        else if (key == "timestep") fields >> p->timeStep;
+        else if (key == "simiterations") fields >> p->simIterations;
+        else if (key == "substeps") fields >> p->subSteps;
+        else if (key == "smoothlen") fields >> p->h;
+        else if (key == "gridbuffersize") fields >> p->gridBufSize;
+        else if (key == "restdensity") fields >> p->restDensity;
+        else if (key == "epsilon") fields >> p->epsilon;
+        else if (key == "garvity") fields >> p->garvity;
+        else if (key == "vorticityfactor") fields >> p->vorticityFactor;
+        else if (key == "viscosityfactor") fields >> p->viscosityFactor;
+        else if (key == "surfacetenstionk") fields >> p->surfaceTenstionK;
+        else if (key == "surfacetenstiondist") fields >> p->surfaceTenstionDist;
+        else if (key == "setupspacing") fields >> p->setupSpacing;
+        else if (key == "segmentsize") fields >> p->segmentSize;
+        else if (key == "sortiterations") fields >> p->sortIterations;
+        else if (key == "particlerendersize") fields >> p->particleRenderSize;
+        else if (key == "enablecachedbuffers") fields >> p->EnableCachedBuffers;
+        // Keys added by this library.
+        else if (key == "gravityx") { fields >> p->gravityX; p->gravityVectorEnable = 1; }
+        else if (key == "gravityy") { fields >> p->gravityY; p->gravityVectorEnable = 1; }
+        else if (key == "gravityz") { fields >> p->gravityZ; p->gravityVectorEnable = 1; }
+        else if (key == "boxclamp") fields >> p->boxClamp;
+        else {
+            std::cerr << "Unknown parameter " << key << std::endl << "Leaving it out." << std::endl;
+            ++nUnknown;
+        }
+    }
+    apply_computed_fields(p);
+    if (unknown) *unknown = nUnknown;
+    return PBF_OK;
+}
+
+// Simulation::CreateParticles (src/Simulation.cpp:71-101): a cube of
+// ceil(cbrt(N)) particles per axis at spacing h*setupSpacing, index i mapped
+// to (x, y, z) = ((i/P) % P, i % P, (i/P^2) % P).
+extern "C" int pbf_reference_lattice(const PbfParameters* p, float* pos) {
+    if (!p || !pos) return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_reference_lattice: NULL argument");
+    const unsigned N = p->particleCount;
+    const int P = (int)std::ceil(std::pow((double)N, 1 / 3.0));
+    const float d = p->h * p->setupSpacing;
+    const float offX = (1.0f - P * d) / 2.0f;
+    const float offY = 0.3f;
+    const float offZ = (1.0f - P * d) / 2.0f;
+    for (unsigned i = 0; i < N; ++i) {
+        unsigned x = ((unsigned)(i / std::pow((double)P, 1.0)) % P);
+        unsigned y = ((unsigned)(i / std::pow((double)P, 0.0)) % P);
+        unsigned z = ((unsigned)(i / std::pow((double)P, 2.0)) % P);
+        pos[4 * (size_t)i + 0] = offX + x * d;
+        pos[4 * (size_t)i + 1] = offY + y * d;
+        pos[4 * (size_t)i + 2] = offZ + z * d;
+        pos[4 * (size_t)i + 3] = 0.0f;
+    }
+    return PBF_OK;
+}
+
+// Jittered block lattice used by the dam-break scenarios.  The uniform draw
+// takes the top 53 bits of each 64-bit Mersenne Twister output, so the values
+// do not depend on the standard library's distribution classes.
+extern "C" int pbf_scene_block(int nx, int ny, int nz, float spacing, float ox, float oy, float oz,
+                               float jitter, uint64_t seed, float* pos) {
+    if (!pos || nx <= 0 || ny <= 0 || nz <= 0)
+        return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_scene_block: bad arguments");
+    std::mt19937_64 rng(seed);
+    const double s = spacing, j = jitter;
+    const double o[3] = {ox, oy, oz};
+    size_t i = 0;
+    for (int iz = 0; iz < nz; ++iz)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int ix = 0; ix < nx; ++ix, ++i) {
+                const int idx[3] = {ix, iy, iz};
+                for (int c = 0; c < 3; ++c) {
+                    double u = (double)(rng() >> 11) * 0x1.0p-53;  // [0, 1)
+                    pos[4 * i + c] = (float)(o[c] + idx[c] * s + (2.0 * u - 1.0) * j);
+                }
+                pos[4 * i + 3] = 0.0f;
+            }
+    return PBF_OK;
+}

@@ -1,0 +1,650 @@
+// pbf_capi.cu — the C-ABI (include/pbf_capi.h): context lifetime, device
+// buffers, the substep orchestration of Simulation::Step
+// (src/Simulation.cpp:554-621) and the parity hooks.
+//
+// Buffer roles within one substep (N particles; index in brackets):
+//   predict      pos[P] vel[V]            -> pred[0], keys[0], perm[0]
+//   sort         keys/perm ping-pong      -> keys[k], perm[k]
+//   gather       pos[P] pred[0]           -> pos[P^1], pred[1]   (sortParticles)
+//   cells        keys[k]                  -> cells
+//   friends      pred[1] cells            -> list, counts; cells reset
+//   iterations   pred[1] -> pred[0] (lambda packed in w) -> pred[1]
+//   velocities   pred[1] pos[P^1]         -> pos[P], vel[V]
+//   viscosity    pred[1] vel[V]           -> vel[V^1], omega
+//   vorticity    vel[V^1] omega           -> vel[V]
+// so an unpaused substep starts and ends with the same roles and one
+// captured CUDA graph replays every substep.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "pbf_capi.h"
+#include "pbf_internal.h"
+
+struct pbf_ctx {
+    PbfParameters params{};
+    int device = 0;
+    int n = 0;
+    cudaStream_t stream = nullptr;
+    bool buffersReady = false, cellsReady = false, kernelsReady = false;
+    int paused = 0;
+    std::string lastError;
+
+    float4* pos[2] = {nullptr, nullptr};
+    float4* pred[2] = {nullptr, nullptr};
+    float4* vel[2] = {nullptr, nullptr};
+    float4* omega = nullptr;
+    float* density = nullptr;
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* perm[2] = {nullptr, nullptr};
+    uint32_t* hist = nullptr;
+    uint32_t* cells = nullptr;
+    uint32_t* list = nullptr;
+    uint32_t* counts = nullptr;
+    int* errWord = nullptr;
+    size_t histWords = 0;
+    uint32_t cellsWords = 0;  // gridBufSize the cell table was allocated for
+    int listSlots = 0;
+
+    pbf::SortPlan plan;
+    pbf::DevConsts consts{};
+    int curPos = 0, curVel = 0, curPred = 1, keysIdx = 0;
+    bool stepped = false;
+
+    bool useGraph = true;
+    cudaGraphExec_t graph = nullptr;
+    int graphPos = -1;
+    size_t graphNodes = 0;
+    uint64_t launches = 0;
+
+    bool stageTiming = false;
+    std::vector<std::string> stageNames;
+    std::vector<float> stageMs;
+};
+
+namespace pbf {
+
+thread_local std::string tls_error = "no error";
+
+int fail(pbf_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->lastError = msg;
+    tls_error = msg;
+    return code;
+}
+
+// The -D constants of src/Simulation.cpp:169-183 and the two powers of
+// compute_delta.cl:81-82, formed on the host.  POLY6_FACTOR and
+// GRAD_SPIKY_FACTOR go through the reference's text round trip: the double
+// value printed with 6 significant digits and read back as a float literal.
+static float six_digit_literal(double v) {
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "%.6g", v);
+    return std::strtof(buf, nullptr);
+}
+
+DevConsts make_consts(const PbfParameters& p, int n) {
+    DevConsts c{};
+    const double kPi = 3.14159265358979323846;
+    c.dt = p.timeStep;
+    c.h = p.h;
+    c.h2 = p.h_2;
+    c.minR = 0.3f * p.h;
+    c.hMinusMinR = p.h - c.minR;
+    c.poly6 = six_digit_literal(315.0f / (64.0f * kPi * std::pow((double)p.h, 9.0)));
+    c.gradSpiky = six_digit_literal(45.0f / (kPi * std::pow((double)p.h, 6.0)));
+    c.negGradSpiky = -c.gradSpiky;
+    const float qh = p.surfaceTenstionDist * p.h;
+    const float q2 = (float)((double)qh * (double)qh);
+    const float d = p.h_2 - q2;
+    c.poly6q = (float)((double)d * (double)d * (double)d);
+    c.rho0 = p.restDensity;
+    c.rho0sq = p.restDensity * p.restDensity;
+    c.eps = p.epsilon;
+    c.K = p.surfaceTenstionK;
+    c.visc = p.viscosityFactor;
+    c.vort = p.vorticityFactor;
+    if (p.gravityVectorEnable) { c.gx = p.gravityX; c.gy = p.gravityY; c.gz = p.gravityZ; }
+    else { c.gx = 0.0f; c.gy = -p.garvity; c.gz = 0.0f; }
+    c.lo[0] = p.xMin; c.lo[1] = p.yMin; c.lo[2] = p.zMin;
+    c.hi[0] = p.xMax; c.hi[1] = p.yMax; c.hi[2] = p.zMax;
+    c.clamp = p.boxClamp ? 1 : 0;
+    c.circles = (int)p.friendsCircles;
+    c.perCircle = (int)p.particlesPerCircle;
+    c.grid = p.gridBufSize;
+    c.n = n;
+    return c;
+}
+
+}  // namespace pbf
+
+namespace {
+
+using pbf::fail;
+
+#define PBF_CUDA(ctx, call)                                                                      \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail((ctx), PBF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T> int dev_alloc(pbf_ctx* ctx, T** p, size_t count) {
+    if (*p) { cudaFree(*p); *p = nullptr; }
+    if (count == 0) count = 1;
+    PBF_CUDA(ctx, cudaMalloc((void**)p, sizeof(T) * count));
+    return PBF_OK;
+}
+
+template <typename T> void dev_free(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+void drop_graph(pbf_ctx* ctx) {
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+    ctx->graphPos = -1;
+}
+
+int validate(pbf_ctx* ctx, const PbfParameters& p) {
+    if (p.particleCount < 1 || p.particleCount > PBF_MAX_PARTICLES)
+        return fail(ctx, PBF_ERR_INVALID, "particleCount must be in [1, 2^26]");
+    if (p.friendsCircles < 1 || p.friendsCircles > PBF_MAX_CIRCLES)
+        return fail(ctx, PBF_ERR_INVALID, "friendsCircles must be in [1, 8]");
+    if (p.particlesPerCircle < 1 || p.particlesPerCircle > PBF_MAX_PER_CIRCLE)
+        return fail(ctx, PBF_ERR_INVALID, "particlesPerCircle must be in [1, 64]");
+    if (p.gridBufSize < 1 || p.gridBufSize > (1u << 30))
+        return fail(ctx, PBF_ERR_INVALID, "gridBufSize must be in [1, 2^30]");
+    if (!(p.h > 0.0f) || !(p.timeStep > 0.0f))
+        return fail(ctx, PBF_ERR_INVALID, "SmoothLen and TimeStep must be positive");
+    if (p.simIterations > 1000) return fail(ctx, PBF_ERR_INVALID, "simIterations must be <= 1000");
+    return PBF_OK;
+}
+
+// ------------------------------------------------------------- the step --
+struct StageClock {
+    pbf_ctx* ctx;
+    std::vector<std::pair<int, cudaEvent_t>> marks;  // (stage index, event recorded before it)
+    int stage(const char* name) {
+        if (!ctx->stageTiming) return PBF_OK;
+        int idx = -1;
+        for (size_t k = 0; k < ctx->stageNames.size(); ++k)
+            if (ctx->stageNames[k] == name) idx = (int)k;
+        if (idx < 0) { ctx->stageNames.push_back(name); ctx->stageMs.push_back(0.0f); idx = (int)ctx->stageNames.size() - 1; }
+        cudaEvent_t e;
+        PBF_CUDA(ctx, cudaEventCreate(&e));
+        PBF_CUDA(ctx, cudaEventRecord(e, ctx->stream));
+        marks.emplace_back(idx, e);
+        return PBF_OK;
+    }
+    int finish() {
+        if (!ctx->stageTiming || marks.empty()) return PBF_OK;
+        cudaEvent_t end;
+        PBF_CUDA(ctx, cudaEventCreate(&end));
+        PBF_CUDA(ctx, cudaEventRecord(end, ctx->stream));
+        PBF_CUDA(ctx, cudaEventSynchronize(end));
+        for (size_t k = 0; k < marks.size(); ++k) {
+            float ms = 0.0f;
+            cudaEvent_t next = k + 1 < marks.size() ? marks[k + 1].second : end;
+            cudaEventElapsedTime(&ms, marks[k].second, next);
+            ctx->stageMs[marks[k].first] += ms;
+        }
+        for (auto& m : marks) cudaEventDestroy(m.second);
+        cudaEventDestroy(end);
+        marks.clear();
+        return PBF_OK;
+    }
+};
+
+__global__ void pack_density_kernel(int n, float4* pred, const float* density) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pred[i].w = density[i];
+}
+
+// Enqueue one Simulation::Step on the context's stream.
+int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
+    const pbf::DevConsts& c = ctx->consts;
+    cudaStream_t s = ctx->stream;
+    const int P = ctx->curPos, V = ctx->curVel;
+    const bool paused = ctx->paused != 0;
+    uint64_t launched = 0;
+    auto mark = [&](const char* name) { return clock ? clock->stage(name) : PBF_OK; };
+
+    mark("predictPositions");
+    pbf::launch_predict_keys(c, ctx->pos[P], ctx->vel[V], ctx->pred[0], ctx->keys[0], ctx->perm[0], paused, s);
+    ++launched;
+    int sortedPos = P, sortedPred = 0;
+    if (!paused) {
+        mark("radixsort");
+        ctx->keysIdx = pbf::launch_radix_sort(ctx->plan, ctx->keys, ctx->perm, ctx->hist, nullptr, nullptr, nullptr,
+                                              nullptr, s);
+        launched += pbf::radix_sort_launches(ctx->plan);
+        mark("sortParticles");
+        pbf::launch_gather_sorted(c.n, ctx->perm[ctx->keysIdx], ctx->pos[P], ctx->pred[0], ctx->pos[P ^ 1],
+                                  ctx->pred[1], s);
+        ++launched;
+        sortedPos = P ^ 1;
+        sortedPred = 1;
+    }
+    const uint32_t* keys = ctx->keys[ctx->keysIdx];
+    mark("updateCells");
+    pbf::launch_update_cells(c.n, keys, ctx->cells, s);
+    mark("buildFriendsList");
+    pbf::launch_build_friends(c, ctx->pred[sortedPred], ctx->cells, ctx->list, ctx->counts, ctx->errWord, s);
+    mark("resetPartList");
+    pbf::launch_reset_cells(c.n, keys, ctx->cells, s);
+    launched += 3;
+    int a = sortedPred;
+    const unsigned iters = ctx->params.simIterations;
+    for (unsigned it = 0; it < iters; ++it) {
+        mark("computeScaling");
+        pbf::launch_compute_scaling(c, ctx->pred[a], ctx->pred[a ^ 1], ctx->density, ctx->list, ctx->counts, s);
+        mark("computeDelta");
+        pbf::launch_compute_delta(c, ctx->pred[a ^ 1], ctx->pred[a], ctx->density, ctx->list, ctx->counts,
+                                  it + 1 == iters, s);
+        launched += 2;
+    }
+    if (iters == 0) {  // packData with the density buffer as it stands (src/Simulation.cpp:591)
+        mark("packData");
+        pack_density_kernel<<<(c.n + 255) / 256, 256, 0, s>>>(c.n, ctx->pred[a], ctx->density);
+        ++launched;
+    }
+    mark("updateVelocities");
+    pbf::launch_update_velocities(c, ctx->pred[a], ctx->pos[sortedPos], ctx->pos[sortedPos ^ 1], ctx->vel[V], s);
+    mark("applyViscosity");
+    pbf::launch_apply_viscosity(c, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], ctx->omega, ctx->list, ctx->counts, s);
+    mark("applyVorticity");
+    pbf::launch_apply_vorticity(c, ctx->pred[a], ctx->omega, ctx->vel[V ^ 1], ctx->vel[V], ctx->list, ctx->counts, s);
+    launched += 3;
+    PBF_CUDA(ctx, cudaGetLastError());
+    ctx->curPos = sortedPos ^ 1;
+    ctx->curPred = a;
+    ctx->launches += launched;
+    return PBF_OK;
+}
+
+int capture_graph(pbf_ctx* ctx) {
+    drop_graph(ctx);
+    const int savedPos = ctx->curPos, savedPred = ctx->curPred, savedKeys = ctx->keysIdx;
+    const uint64_t savedLaunches = ctx->launches;
+    cudaGraph_t g = nullptr;
+    PBF_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_substep(ctx, nullptr);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->curPos = savedPos;
+    ctx->curPred = savedPred;
+    ctx->keysIdx = savedKeys;
+    ctx->launches = savedLaunches;
+    if (rc != PBF_OK) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return fail(ctx, PBF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    e = cudaGraphInstantiate(&ctx->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { ctx->graph = nullptr; return fail(ctx, PBF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
+    ctx->graphPos = savedPos;
+    ctx->graphNodes = nodes;
+    return PBF_OK;
+}
+
+int check_ready(pbf_ctx* ctx) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    if (!ctx->buffersReady || !ctx->cellsReady || !ctx->kernelsReady)
+        return fail(ctx, PBF_ERR_STATE, "InitBuffers, InitCells and InitKernels must run before stepping");
+    return PBF_OK;
+}
+
+int read_error_word(pbf_ctx* ctx) {
+    int word = 0;
+    PBF_CUDA(ctx, cudaMemcpyAsync(&word, ctx->errWord, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (word) {
+        PBF_CUDA(ctx, cudaMemsetAsync(ctx->errWord, 0, sizeof(int), ctx->stream));
+        return fail(ctx, PBF_ERR_DEVICE_FLAG, "a kernel reported an inconsistent cell table (error word " + std::to_string(word) + ")");
+    }
+    return PBF_OK;
+}
+
+}  // namespace
+
+// ================================================================ C-ABI ==
+extern "C" {
+
+const char* pbf_last_error(const pbf_ctx* ctx) {
+    return ctx ? ctx->lastError.c_str() : pbf::tls_error.c_str();
+}
+
+int pbf_create(const PbfParameters* params, int device, pbf_ctx** out) {
+    if (!params || !out) return fail(nullptr, PBF_ERR_INVALID, "pbf_create: NULL argument");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0)
+        return fail(nullptr, PBF_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (device < 0 || device >= count) return fail(nullptr, PBF_ERR_INVALID, "pbf_create: device ordinal out of range");
+    std::unique_ptr<pbf_ctx> ctx(new pbf_ctx());
+    ctx->params = *params;
+    ctx->device = device;
+    PBF_CUDA(nullptr, cudaSetDevice(device));
+    PBF_CUDA(nullptr, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->errWord, sizeof(int)));
+    PBF_CUDA(nullptr, cudaMemset(ctx->errWord, 0, sizeof(int)));
+    *out = ctx.release();
+    return PBF_OK;
+}
+
+int pbf_destroy(pbf_ctx* ctx) {
+    if (!ctx) return PBF_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    drop_graph(ctx);
+    for (int k = 0; k < 2; ++k) {
+        dev_free(ctx->pos[k]); dev_free(ctx->pred[k]); dev_free(ctx->vel[k]);
+        dev_free(ctx->keys[k]); dev_free(ctx->perm[k]);
+    }
+    dev_free(ctx->omega); dev_free(ctx->density); dev_free(ctx->hist); dev_free(ctx->cells);
+    dev_free(ctx->list); dev_free(ctx->counts); dev_free(ctx->errWord);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return PBF_OK;
+}
+
+int pbf_init_buffers(pbf_ctx* ctx, const float* init_pos, const float* init_vel) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    const PbfParameters& p = ctx->params;
+    if (p.particleCount < 1 || p.particleCount > PBF_MAX_PARTICLES)
+        return fail(ctx, PBF_ERR_INVALID, "particleCount must be in [1, 2^26]");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    drop_graph(ctx);
+    const int n = (int)p.particleCount;
+    ctx->n = n;
+    int rc;
+    for (int k = 0; k < 2; ++k) {
+        if ((rc = dev_alloc(ctx, &ctx->pos[k], n)) || (rc = dev_alloc(ctx, &ctx->pred[k], n)) ||
+            (rc = dev_alloc(ctx, &ctx->vel[k], n)) || (rc = dev_alloc(ctx, &ctx->keys[k], n)) ||
+            (rc = dev_alloc(ctx, &ctx->perm[k], n)))
+            return rc;
+        PBF_CUDA(ctx, cudaMemset(ctx->keys[k], 0, 4 * (size_t)n));
+        PBF_CUDA(ctx, cudaMemset(ctx->pred[k], 0, 16 * (size_t)n));
+    }
+    if ((rc = dev_alloc(ctx, &ctx->omega, n)) || (rc = dev_alloc(ctx, &ctx->density, n))) return rc;
+    PBF_CUDA(ctx, cudaMemset(ctx->omega, 0, 16 * (size_t)n));
+    PBF_CUDA(ctx, cudaMemset(ctx->density, 0, 4 * (size_t)n));
+    ctx->curPos = 0; ctx->curVel = 0; ctx->curPred = 1; ctx->keysIdx = 0; ctx->stepped = false;
+    std::vector<float> host;
+    const float* src = init_pos;
+    if (!src) {
+        host.assign(4 * (size_t)n, 0.0f);
+        if ((rc = pbf_reference_lattice(&p, host.data())) != PBF_OK) return fail(ctx, rc, pbf_last_error(nullptr));
+        src = host.data();
+    }
+    PBF_CUDA(ctx, cudaMemcpy(ctx->pos[0], src, 16 * (size_t)n, cudaMemcpyHostToDevice));
+    if (init_vel) PBF_CUDA(ctx, cudaMemcpy(ctx->vel[0], init_vel, 16 * (size_t)n, cudaMemcpyHostToDevice));
+    else PBF_CUDA(ctx, cudaMemset(ctx->vel[0], 0, 16 * (size_t)n));
+    PBF_CUDA(ctx, cudaMemset(ctx->vel[1], 0, 16 * (size_t)n));
+    ctx->buffersReady = true;
+    ctx->kernelsReady = false;
+    return PBF_OK;
+}
+
+int pbf_init_cells(pbf_ctx* ctx) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers must run before InitCells");
+    const PbfParameters& p = ctx->params;
+    if (p.gridBufSize < 1 || p.gridBufSize > (1u << 30)) return fail(ctx, PBF_ERR_INVALID, "gridBufSize must be in [1, 2^30]");
+    if (p.friendsCircles < 1 || p.friendsCircles > PBF_MAX_CIRCLES || p.particlesPerCircle < 1 ||
+        p.particlesPerCircle > PBF_MAX_PER_CIRCLE)
+        return fail(ctx, PBF_ERR_INVALID, "friendsCircles must be in [1, 8] and particlesPerCircle in [1, 64]");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    drop_graph(ctx);
+    int rc;
+    if ((rc = dev_alloc(ctx, &ctx->cells, 2 * (size_t)p.gridBufSize))) return rc;
+    PBF_CUDA(ctx, cudaMemset(ctx->cells, 0xFF, 8 * (size_t)p.gridBufSize));
+    ctx->cellsWords = p.gridBufSize;
+    ctx->listSlots = (int)(p.friendsCircles * p.particlesPerCircle);
+    if ((rc = dev_alloc(ctx, &ctx->list, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->counts, ctx->n)))
+        return rc;
+    PBF_CUDA(ctx, cudaMemset(ctx->counts, 0, 4 * (size_t)ctx->n));
+    ctx->cellsReady = true;
+    ctx->kernelsReady = false;
+    return PBF_OK;
+}
+
+int pbf_load_force_masks(pbf_ctx* ctx, const uint32_t* mask, int width, int height) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    (void)width; (void)height;
+    if (mask) return fail(ctx, PBF_ERR_UNSUPPORTED, "force-plane masks other than the empty mask are not supported");
+    return PBF_OK;
+}
+
+int pbf_init_kernels(pbf_ctx* ctx) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    if (!ctx->buffersReady || !ctx->cellsReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers and InitCells must run before InitKernels");
+    int rc = validate(ctx, ctx->params);
+    if (rc) return rc;
+    if ((int)ctx->params.particleCount != ctx->n) return fail(ctx, PBF_ERR_INVALID, "particleCount changed since InitBuffers");
+    if (ctx->params.gridBufSize != ctx->cellsWords ||
+        (int)(ctx->params.friendsCircles * ctx->params.particlesPerCircle) != ctx->listSlots)
+        return fail(ctx, PBF_ERR_INVALID, "gridBufSize or friend limits changed since InitCells");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    drop_graph(ctx);
+    ctx->consts = pbf::make_consts(ctx->params, ctx->n);
+    ctx->plan = pbf::make_sort_plan(ctx->n, ctx->params.gridBufSize);
+    if (ctx->plan.histWords != ctx->histWords) {
+        if ((rc = dev_alloc(ctx, &ctx->hist, ctx->plan.histWords))) return rc;
+        ctx->histWords = ctx->plan.histWords;
+    }
+    ctx->kernelsReady = true;
+    return PBF_OK;
+}
+
+int pbf_set_params(pbf_ctx* ctx, const PbfParameters* params) {
+    if (!ctx || !params) return fail(ctx, PBF_ERR_INVALID, "pbf_set_params: NULL argument");
+    int rc = validate(ctx, *params);
+    if (rc) return rc;
+    if (ctx->buffersReady && (int)params->particleCount != ctx->n)
+        return fail(ctx, PBF_ERR_INVALID, "pbf_set_params cannot change particleCount; re-run InitBuffers");
+    if (ctx->cellsReady && (params->gridBufSize != ctx->cellsWords ||
+                            (int)(params->friendsCircles * params->particlesPerCircle) != ctx->listSlots))
+        return fail(ctx, PBF_ERR_INVALID, "pbf_set_params cannot change gridBufSize or friend limits; re-run InitCells");
+    ctx->params = *params;
+    if (ctx->kernelsReady) {
+        drop_graph(ctx);
+        ctx->consts = pbf::make_consts(ctx->params, ctx->n);
+    }
+    return PBF_OK;
+}
+
+int pbf_set_pause(pbf_ctx* ctx, int paused) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    ctx->paused = paused ? 1 : 0;
+    return PBF_OK;
+}
+
+int pbf_step_async(pbf_ctx* ctx, int substeps) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (substeps < 0) return fail(ctx, PBF_ERR_INVALID, "substeps must be >= 0");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    StageClock clock{ctx, {}};
+    if (ctx->stageTiming) std::fill(ctx->stageMs.begin(), ctx->stageMs.end(), 0.0f);
+    for (int k = 0; k < substeps; ++k) {
+        const bool graphOk = ctx->useGraph && !ctx->paused && !ctx->stageTiming;
+        if (graphOk) {
+            if (!ctx->graph || ctx->graphPos != ctx->curPos)
+                if ((rc = capture_graph(ctx))) return rc;
+            PBF_CUDA(ctx, cudaGraphLaunch(ctx->graph, ctx->stream));
+            // the replayed substep has the captured buffer roles
+            ctx->keysIdx = ctx->plan.passes & 1;
+            ctx->curPred = 1;
+            ctx->launches += ctx->graphNodes;
+        } else {
+            if ((rc = enqueue_substep(ctx, ctx->stageTiming ? &clock : nullptr))) return rc;
+        }
+        ctx->stepped = true;
+    }
+    if (ctx->stageTiming) return clock.finish();
+    return PBF_OK;
+}
+
+int pbf_synchronize(pbf_ctx* ctx) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    PBF_CUDA(ctx, cudaGetLastError());
+    return read_error_word(ctx);
+}
+
+int pbf_step(pbf_ctx* ctx, int substeps) {
+    int rc = pbf_step_async(ctx, substeps);
+    if (rc) return rc;
+    return pbf_synchronize(ctx);
+}
+
+int pbf_read_state(pbf_ctx* ctx, float* pos, float* vel, float* pred) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers has not run");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = 16 * (size_t)ctx->n;
+    if (pos) PBF_CUDA(ctx, cudaMemcpyAsync(pos, ctx->pos[ctx->curPos], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vel) PBF_CUDA(ctx, cudaMemcpyAsync(vel, ctx->vel[ctx->curVel], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (pred) PBF_CUDA(ctx, cudaMemcpyAsync(pred, ctx->pred[ctx->curPred], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PBF_OK;
+}
+
+int pbf_write_state(pbf_ctx* ctx, const float* pos, const float* vel) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers has not run");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = 16 * (size_t)ctx->n;
+    if (pos) PBF_CUDA(ctx, cudaMemcpyAsync(ctx->pos[ctx->curPos], pos, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (vel) PBF_CUDA(ctx, cudaMemcpyAsync(ctx->vel[ctx->curVel], vel, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PBF_OK;
+}
+
+int pbf_device_positions(pbf_ctx* ctx, void** dptr) {
+    if (!ctx || !dptr) return fail(ctx, PBF_ERR_INVALID, "pbf_device_positions: NULL argument");
+    if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers has not run");
+    *dptr = ctx->pos[ctx->curPos];
+    return PBF_OK;
+}
+
+int pbf_get_stream(pbf_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return fail(ctx, PBF_ERR_INVALID, "pbf_get_stream: NULL argument");
+    *stream = (void*)ctx->stream;
+    return PBF_OK;
+}
+
+int pbf_sort_state(pbf_ctx* ctx, const float* pred, uint32_t* keys, uint32_t* perm, uint32_t* cells) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!pred) return fail(ctx, PBF_ERR_INVALID, "pbf_sort_state: pred is NULL");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int n = ctx->n;
+    const uint32_t grid = ctx->params.gridBufSize;
+    float4* dPred = nullptr;
+    uint32_t *k[2] = {nullptr, nullptr}, *pm[2] = {nullptr, nullptr}, *dCells = nullptr, *dHist = nullptr;
+    auto cleanup = [&] {
+        cudaFree(dPred); cudaFree(k[0]); cudaFree(k[1]); cudaFree(pm[0]); cudaFree(pm[1]);
+        cudaFree(dCells); cudaFree(dHist);
+    };
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaMalloc((void**)&dPred, 16 * (size_t)n)) || (e = cudaMalloc((void**)&k[0], 4 * (size_t)n)) ||
+        (e = cudaMalloc((void**)&k[1], 4 * (size_t)n)) || (e = cudaMalloc((void**)&pm[0], 4 * (size_t)n)) ||
+        (e = cudaMalloc((void**)&pm[1], 4 * (size_t)n)) || (e = cudaMalloc((void**)&dCells, 8 * (size_t)grid)) ||
+        (e = cudaMalloc((void**)&dHist, 4 * ctx->plan.histWords))) {
+        cleanup();
+        return fail(ctx, PBF_ERR_CUDA, std::string("pbf_sort_state: ") + cudaGetErrorString(e));
+    }
+    cudaStream_t s = ctx->stream;
+    cudaMemcpyAsync(dPred, pred, 16 * (size_t)n, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(dCells, 0xFF, 8 * (size_t)grid, s);
+    pbf::launch_compute_keys(ctx->consts, dPred, k[0], pm[0], s);
+    const int r = pbf::launch_radix_sort(ctx->plan, k, pm, dHist, nullptr, nullptr, nullptr, nullptr, s);
+    pbf::launch_update_cells(n, k[r], dCells, s);
+    const uint32_t nKeys = ((uint32_t)n + 2047u) / 2048u * 2048u;
+    if (keys) {
+        cudaMemcpyAsync(keys, k[r], 4 * (size_t)n, cudaMemcpyDeviceToHost, s);
+    }
+    if (perm) cudaMemcpyAsync(perm, pm[r], 4 * (size_t)n, cudaMemcpyDeviceToHost, s);
+    if (cells) cudaMemcpyAsync(cells, dCells, 8 * (size_t)grid, cudaMemcpyDeviceToHost, s);
+    e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    cleanup();
+    if (e != cudaSuccess) return fail(ctx, PBF_ERR_CUDA, std::string("pbf_sort_state: ") + cudaGetErrorString(e));
+    // The reference sorts IntCeil(N, 2048) keys, the tail padded with
+    // 2147483646 (radixsort.cl:17), which sorts after every cell key.
+    for (uint32_t i = (uint32_t)n; i < nKeys; ++i) {
+        if (keys) keys[i] = 2147483646u;
+        if (perm) perm[i] = i;
+    }
+    return PBF_OK;
+}
+
+int pbf_read_friends(pbf_ctx* ctx, uint32_t* counts, uint32_t* list, int list_slots) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!ctx->stepped) return fail(ctx, PBF_ERR_STATE, "no substep has run yet");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int n = ctx->n;
+    if (counts) {
+        std::vector<uint32_t> packed(n);
+        PBF_CUDA(ctx, cudaMemcpyAsync(packed.data(), ctx->counts, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+        PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int i = 0; i < n; ++i) { counts[2 * i] = packed[i] & 0xFFFFu; counts[2 * i + 1] = packed[i] >> 16; }
+    }
+    if (list && list_slots > 0) {
+        const int slots = std::min(list_slots, ctx->listSlots);
+        PBF_CUDA(ctx, cudaMemcpyAsync(list, ctx->list, 4 * (size_t)slots * n, cudaMemcpyDeviceToHost, ctx->stream));
+        PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return PBF_OK;
+}
+
+int pbf_enable_stage_timing(pbf_ctx* ctx, int enable) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    ctx->stageTiming = enable != 0;
+    ctx->stageNames.clear();
+    ctx->stageMs.clear();
+    return PBF_OK;
+}
+
+int pbf_stage_timings(pbf_ctx* ctx, float* ms, int capacity, int* count, char* names, size_t names_len) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    const int k = (int)ctx->stageNames.size();
+    if (count) *count = k;
+    if (ms)
+        for (int i = 0; i < std::min(k, capacity); ++i) ms[i] = ctx->stageMs[i];
+    if (names && names_len) {
+        std::string joined;
+        for (int i = 0; i < k; ++i) { if (i) joined += '\n'; joined += ctx->stageNames[i]; }
+        std::snprintf(names, names_len, "%s", joined.c_str());
+    }
+    return PBF_OK;
+}
+
+int pbf_launch_count(pbf_ctx* ctx, uint64_t* count) {
+    if (!ctx || !count) return fail(ctx, PBF_ERR_INVALID, "pbf_launch_count: NULL argument");
+    *count = ctx->launches;
+    return PBF_OK;
+}
+
+int pbf_use_graph(pbf_ctx* ctx, int enable) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    ctx->useGraph = enable != 0;
+    if (!ctx->useGraph) drop_graph(ctx);
+    return PBF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,73 @@
+// pbf_internal.h — declarations shared by the library's translation units.
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+#include "pbf_capi.h"
+
+#include <cuda_runtime.h>
+
+namespace pbf {
+
+// Constants every solver kernel reads, formed once on the host from the
+// parameters (src/Simulation.cpp:169-183 bakes the same values into the
+// OpenCL build as -D literals).
+struct DevConsts {
+    float dt, h, h2, minR, hMinusMinR;
+    float poly6, gradSpiky, negGradSpiky, poly6q;
+    float rho0, rho0sq, eps, K, visc, vort;
+    float gx, gy, gz;
+    float lo[3], hi[3];
+    int clamp;
+    int circles, perCircle;
+    uint32_t grid;
+    int n;
+};
+
+// Records `msg` as the last error of `ctx` (or of the calling thread when ctx
+// is NULL) and returns `code`.
+int fail(pbf_ctx* ctx, int code, const std::string& msg);
+
+DevConsts make_consts(const PbfParameters& p, int n);
+
+// ---- kernels (pbf_kernels.cu) ----
+void launch_predict_keys(const DevConsts& c, const float4* pos, float4* vel, float4* pred,
+                         uint32_t* keys, uint32_t* perm, int paused, cudaStream_t s);
+void launch_compute_keys(const DevConsts& c, const float4* pred, uint32_t* keys, uint32_t* perm, cudaStream_t s);
+void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred,
+                          float4* posOut, float4* predOut, cudaStream_t s);
+void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
+void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
+void launch_build_friends(const DevConsts& c, const float4* pred, const uint32_t* cells, uint32_t* list,
+                          uint32_t* counts, int* errorWord, cudaStream_t s);
+void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
+                            const uint32_t* list, const uint32_t* counts, cudaStream_t s);
+void launch_compute_delta(const DevConsts& c, const float4* predPacked, float4* predOut, const float* density,
+                          const uint32_t* list, const uint32_t* counts, int lastIteration, cudaStream_t s);
+void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
+                              float4* vel, cudaStream_t s);
+void launch_apply_viscosity(const DevConsts& c, const float4* pred, const float4* velIn, float4* velOut,
+                            float4* omega, const uint32_t* list, const uint32_t* counts, cudaStream_t s);
+void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
+                            float4* velOut, const uint32_t* list, const uint32_t* counts, cudaStream_t s);
+
+// ---- radix sort (pbf_sort.cu) ----
+struct SortPlan {
+    int n = 0;
+    int passes = 0;       // 8-bit digits needed for keys < gridBufSize
+    int tiles = 0;        // ceil(n / kSortTile)
+    size_t histWords = 0; // 256 * tiles
+};
+SortPlan make_sort_plan(int n, uint32_t gridBufSize);
+// Sorts (keys[0], perm[0]) by key, stably, ping-ponging through keys[1] /
+// perm[1]; returns the index (0 or 1) of the buffers holding the result.
+// When posIn/predIn are given, the last pass also writes posOut/predOut
+// gathered through the permutation (the reference's sortParticles).
+int launch_radix_sort(const SortPlan& plan, uint32_t* keys[2], uint32_t* perm[2], uint32_t* hist,
+                      const float4* posIn, const float4* predIn, float4* posOut, float4* predOut,
+                      cudaStream_t s);
+// Kernels launched by one launch_radix_sort call.
+int radix_sort_launches(const SortPlan& plan);
+
+}  // namespace pbf

@@ -1,0 +1,453 @@
+// pbf_kernels.cu — the per-substep PBF stages on sm_103a.
+//
+// Arithmetic contract (shared with the CPU oracle): this file is compiled
+// with --fmad=false, IEEE division and IEEE sqrt, so every float operation
+// below is one correctly rounded IEEE operation, evaluated in the order of
+// the reference kernel it stands for.  With the same inputs the results are
+// bit-identical to a strict IEEE evaluation of the reference's kernels.
+//   dot(a,b)       = (a.x*b.x + a.y*b.y) + a.z*b.z
+//   cross(a,b)     = (a.y*b.z - a.z*b.y, a.z*b.x - a.x*b.z, a.x*b.y - a.y*b.x)
+//   fast_length(a) = sqrtf(dot(a,a))
+//   convert_int    = __float2int_rz (truncating, saturating, NaN -> 0)
+//
+// Data layout in device memory (N particles, all arrays dense):
+//   pos, pred, vel, omega : float4[N]  (16-byte records, coalesced 128-bit I/O)
+//   keys, perm            : uint32[N]
+//   cells                 : uint2[gridBufSize]  (start, inclusive end)
+//   counts                : uint32[N]   low 16 bits: neighbours used by the
+//                           density pass, high 16 bits: by the delta,
+//                           viscosity and vorticity passes
+//   list                  : uint32[slots][N]  slot-major, so that a warp of
+//                           consecutive particles reads one slot coalesced.
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "pbf_internal.h"
+
+namespace pbf {
+namespace {
+
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;  // END_OF_CELL_LIST
+constexpr int kBlock = 256;
+
+inline unsigned blocks_for(int n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+
+// utilities.cl:69-77
+__device__ __forceinline__ uint32_t expand_bits(int xi) {
+    uint32_t x = (uint32_t)xi;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+// utilities.cl:79-87 (the Morton number is non-negative, < 2^30).
+__device__ __forceinline__ uint32_t grid_hash(int x, int y, int z, uint32_t grid) {
+    uint32_t m = expand_bits(x) | (expand_bits(y) << 1) | (expand_bits(z) << 2);
+    return (grid & (grid - 1)) == 0 ? (m & (grid - 1)) : (m % grid);
+}
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return (ax * bx + ay * by) + az * bz;
+}
+
+// ------------------------------------------------------------- predict --
+// predict_positions.cl:8-17 fused with computeKeys (radixsort.cl:7-19).
+__global__ void predict_keys_kernel(DevConsts c, const float4* __restrict__ pos, float4* __restrict__ vel,
+                                    float4* __restrict__ pred, uint32_t* __restrict__ keys,
+                                    uint32_t* __restrict__ perm, int paused) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    float4 v = vel[i];
+    if (!paused) {
+        v.x = v.x + c.dt * c.gx;
+        v.y = v.y + c.dt * c.gy;
+        v.z = v.z + c.dt * c.gz;
+        vel[i] = v;
+    }
+    const float4 p = pos[i];
+    const float4 q = make_float4(p.x + c.dt * v.x, p.y + c.dt * v.y, p.z + c.dt * v.z, p.w + c.dt * v.w);
+    pred[i] = q;
+    if (!paused) {
+        keys[i] = grid_hash(__float2int_rz(q.x / c.h), __float2int_rz(q.y / c.h), __float2int_rz(q.z / c.h), c.grid);
+        perm[i] = (uint32_t)i;
+    }
+}
+
+// radixsort.cl:1-20 alone (keys of given predicted positions, no padding).
+__global__ void compute_keys_kernel(DevConsts c, const float4* __restrict__ pred, uint32_t* __restrict__ keys,
+                                    uint32_t* __restrict__ perm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const float4 q = pred[i];
+    keys[i] = grid_hash(__float2int_rz(q.x / c.h), __float2int_rz(q.y / c.h), __float2int_rz(q.z / c.h), c.grid);
+    perm[i] = (uint32_t)i;
+}
+
+// radixsort.cl:22-37 (velocities are not permuted; they are recomputed
+// before any read, update_velocities.cl:13).
+__global__ void gather_sorted_kernel(int n, const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
+                                     const float4* __restrict__ pred, float4* __restrict__ posOut,
+                                     float4* __restrict__ predOut) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t j = perm[i];
+    posOut[i] = pos[j];
+    predOut[i] = pred[j];
+}
+
+// --------------------------------------------------------------- cells --
+// update_cells.cl:6-25 on a table that holds END_OF_CELL_LIST everywhere.
+__global__ void update_cells_kernel(int n, const uint32_t* __restrict__ keys, uint32_t* __restrict__ cells) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = keys[i];
+    if (i > 0) {
+        const uint32_t kp = keys[i - 1];
+        if (kp != k) {
+            cells[2 * (size_t)k] = (uint32_t)i;
+            cells[2 * (size_t)kp + 1] = (uint32_t)(i - 1);
+        }
+        if (i == n - 1) cells[2 * (size_t)k + 1] = (uint32_t)i;
+    } else {
+        cells[2 * (size_t)k] = 0u;
+    }
+}
+
+// reset_grid.cl:6-14
+__global__ void reset_cells_kernel(int n, const uint32_t* __restrict__ keys, uint2* __restrict__ cells) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    cells[keys[i]] = make_uint2(kEmpty, kEmpty);
+}
+
+// -------------------------------------------------------------- friends --
+// Packed per-circle counters: 8 circles x 8 bits (counts <= 64).
+__device__ __forceinline__ uint32_t byte_of(uint64_t v, int k) { return (uint32_t)(v >> (8 * k)) & 0xFFu; }
+__device__ __forceinline__ uint32_t half_of(uint64_t lo, uint64_t hi, int k) {
+    return (uint32_t)((k < 4 ? lo : hi) >> (16 * (k & 3))) & 0xFFFFu;
+}
+
+// Number of leading circles a pass keeps: circles are visited in order and
+// skipped once processed/total exceeds the threshold (compute_scaling.cl:47-54
+// with 0.6f; compute_delta.cl:97-104, apply_viscosity.cl:25-32 and
+// apply_vorticity.cl:23-30 with 0.5f).
+__device__ __forceinline__ int circles_kept(uint64_t cnt, int C, int total, float threshold) {
+    int processed = 0, kept = 0;
+    for (int k = 0; k < C; ++k) {
+        if (((float)processed) / total > threshold) continue;
+        processed += (int)byte_of(cnt, k);
+        kept = k + 1;
+    }
+    return kept;
+}
+
+// build_friends_list.cl:29-102.  Two scans of the 27 neighbour cells: the
+// first counts friends per circle (dropping those beyond particlesPerCircle,
+// :79-83), the second writes the ones the density pass will read in
+// circle-major order, which is the order every later pass sums in.
+__global__ void __launch_bounds__(kBlock)
+build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* __restrict__ cells,
+                     uint32_t* __restrict__ list, uint32_t* __restrict__ counts, int* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = c.n;
+    if (i >= n) return;
+    const float4 pi = pred[i];
+    const int cx = __float2int_rz(pi.x / c.h), cy = __float2int_rz(pi.y / c.h), cz = __float2int_rz(pi.z / c.h);
+    const int C = c.circles, P = c.perCircle;
+    const float fC = (float)C;
+
+    uint64_t cnt = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        int keptL = 0;
+        uint64_t offLo = 0, offHi = 0, run = 0;
+        if (pass == 1) {
+            int total = 0;
+            for (int k = 0; k < C; ++k) total += (int)byte_of(cnt, k);
+            keptL = circles_kept(cnt, C, total, 0.6f);
+            const int keptD = circles_kept(cnt, C, total, 0.5f);
+            uint32_t acc = 0, nL = 0, nD = 0;
+            for (int k = 0; k < C; ++k) {
+                if (k < 4) offLo |= (uint64_t)acc << (16 * k); else offHi |= (uint64_t)acc << (16 * (k - 4));
+                acc += byte_of(cnt, k);
+                if (k < keptL) nL = acc;
+                if (k < keptD) nD = acc;
+            }
+            counts[i] = nL | (nD << 16);
+            if (keptL == 0) return;
+        }
+        for (int x = -1; x <= 1; ++x)
+            for (int y = -1; y <= 1; ++y)
+                for (int z = -1; z <= 1; ++z) {
+                    const uint2 range = cells[grid_hash(cx + x, cy + y, cz + z, c.grid)];
+                    if (range.x == kEmpty) continue;
+                    const uint32_t last = min(range.y, (uint32_t)(n - 1));
+                    if (range.x > last) { atomicOr(err, 1); continue; }
+                    for (uint32_t j = range.x; j <= last; ++j) {
+                        if ((int)j == i) continue;
+                        const float4 pj = pred[j];
+                        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+                        if (r2 >= c.h2) continue;
+                        const float adj = fmaxf(0.0f, (sqrtf(r2) - c.minR) / c.hMinusMinR);
+                        const int circ = min(__float2int_rz(adj * adj * adj * fC), C - 1);
+                        if (pass == 0) {
+                            if ((int)byte_of(cnt, circ) >= P) continue;
+                            cnt += 1ull << (8 * circ);
+                        } else {
+                            if (circ >= keptL) continue;
+                            const uint32_t r = byte_of(run, circ);
+                            if ((int)r >= P) continue;
+                            run += 1ull << (8 * circ);
+                            const uint32_t slot = half_of(offLo, offHi, circ) + r;
+                            list[(size_t)slot * n + i] = j;
+                        }
+                    }
+                }
+    }
+}
+
+// -------------------------------------------------------------- scaling --
+// compute_scaling.cl:27-112 followed by pack_data.cl (w = lambda).
+__global__ void __launch_bounds__(kBlock)
+compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __restrict__ predPacked,
+                       float* __restrict__ density, const uint32_t* __restrict__ list,
+                       const uint32_t* __restrict__ counts) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = c.n;
+    if (i >= n) return;
+    const float4 pi = pred[i];
+    const uint32_t nl = counts[i] & 0xFFFFu;
+    float ds = 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
+    for (uint32_t s = 0; s < nl; ++s) {
+        const uint32_t j = list[(size_t)s * n + i];
+        const float4 pj = pred[j];
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+        if (r2 < c.h2) {
+            const float rl = sqrtf(r2);
+            const float hr = c.h - rl;
+            const float sc = c.gradSpiky * hr * hr;
+            const float g0 = (sc * rx) / rl, g1 = (sc * ry) / rl, g2 = (sc * rz) / rl;
+            const float d = c.h2 - r2;
+            ds = ds + d * d * d;
+            gsk = gsk + dot3(g0, g1, g2, g0, g1, g2);
+            gx = gx + g0;
+            gy = gy + g1;
+            gz = gz + g2;
+        }
+    }
+    ds = ds * c.poly6;
+    density[i] = ds;
+    gsk = gsk + dot3(gx, gy, gz, gx, gy, gz);
+    const float constraint = (ds / c.rho0) - 1.0f;
+    const float lambda = -1.0f * constraint / (gsk / c.rho0sq + c.eps);
+    predPacked[i] = make_float4(pi.x, pi.y, pi.z, lambda);
+}
+
+// ---------------------------------------------------------------- delta --
+// compute_delta.cl:54-185 (force planes: identity for an all-zero mask) with
+// the optional box clamp on `future`, then update_predicted.cl.  After the
+// last iteration w carries the density (pack_data.cl with the density source,
+// src/Simulation.cpp:591).
+__global__ void __launch_bounds__(kBlock)
+compute_delta_kernel(DevConsts c, const float4* __restrict__ pp, float4* __restrict__ predOut,
+                     const float* __restrict__ density, const uint32_t* __restrict__ list,
+                     const uint32_t* __restrict__ counts, int lastIteration) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = c.n;
+    if (i >= n) return;
+    const float4 pi = pp[i];
+    const uint32_t nd = counts[i] >> 16;
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    for (uint32_t s = 0; s < nd; ++s) {
+        const uint32_t j = list[(size_t)s * n + i];
+        const float4 pj = pp[j];
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+        if (r2 < c.h2) {
+            const float rl = sqrtf(r2);
+            const float hr = c.h - rl;
+            const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
+            const float d = c.h2 - r2;
+            const float p6 = d * d * d;
+            const float rq = p6 / c.poly6q;
+            const float scorr = c.K * rq * rq * rq * rq;
+            const float a = pi.w + pj.w + scorr;
+            sx = sx + a * g0;
+            sy = sy + a * g1;
+            sz = sz + a * g2;
+        }
+    }
+    float fx = pi.x + (c.negGradSpiky * sx) / c.rho0;
+    float fy = pi.y + (c.negGradSpiky * sy) / c.rho0;
+    float fz = pi.z + (c.negGradSpiky * sz) / c.rho0;
+    if (c.clamp) {
+        fx = fx < c.lo[0] ? c.lo[0] : (fx > c.hi[0] ? c.hi[0] : fx);
+        fy = fy < c.lo[1] ? c.lo[1] : (fy > c.hi[1] ? c.hi[1] : fy);
+        fz = fz < c.lo[2] ? c.lo[2] : (fz > c.hi[2] ? c.hi[2] : fz);
+    }
+    const float dx = fx - pi.x, dy = fy - pi.y, dz = fz - pi.z;
+    predOut[i] = make_float4(pi.x + dx, pi.y + dy, pi.z + dz, lastIteration ? density[i] : pi.w + 0.0f);
+}
+
+// ----------------------------------------------------------- velocities --
+// update_velocities.cl:11-14 (the GL texture write is dropped).
+__global__ void update_velocities_kernel(DevConsts c, const float4* __restrict__ pred,
+                                         const float4* __restrict__ posIn, float4* __restrict__ posOut,
+                                         float4* __restrict__ vel) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    const float4 p = pred[i], q = posIn[i];
+    float4 v = vel[i];
+    v.x = (p.x - q.x) / c.dt;
+    v.y = (p.y - q.y) / c.dt;
+    v.z = (p.z - q.z) / c.dt;
+    vel[i] = v;
+    posOut[i] = make_float4(p.x, p.y, p.z, sqrtf(dot3(v.x, v.y, v.z, v.x, v.y, v.z)));
+}
+
+// apply_viscosity.cl:12-86, every neighbour read from the pre-pass
+// velocities (Jacobi).
+__global__ void __launch_bounds__(kBlock)
+apply_viscosity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ velIn,
+                       float4* __restrict__ velOut, float4* __restrict__ omega,
+                       const uint32_t* __restrict__ list, const uint32_t* __restrict__ counts) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = c.n;
+    if (i >= n) return;
+    const float4 pi = pred[i], vi = velIn[i];
+    const uint32_t nd = counts[i] >> 16;
+    float vsx = 0.0f, vsy = 0.0f, vsz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
+    for (uint32_t s = 0; s < nd; ++s) {
+        const uint32_t j = list[(size_t)s * n + i];
+        const float4 pj = pred[j];
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (r2 < c.h2 && fabsf(pj.w) > 1e-8f) {
+            const float4 vj = velIn[j];
+            const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
+            const float d = c.h2 - r2;
+            const float rl = sqrtf(r2);
+            const float hr = c.h - rl;
+            const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
+            ox = ox + (uy * g2 - uz * g1);
+            oy = oy + (uz * g0 - ux * g2);
+            oz = oz + (ux * g1 - uy * g0);
+            const float d3 = d * d * d;
+            vsx = vsx + ux * d3;
+            vsy = vsy + uy * d3;
+            vsz = vsz + uz * d3;
+        }
+    }
+    vsx = vsx * c.poly6;
+    vsy = vsy * c.poly6;
+    vsz = vsz * c.poly6;
+    velOut[i] = make_float4(vi.x + c.visc * vsx, vi.y + c.visc * vsy, vi.z + c.visc * vsz, vi.w + c.visc * 0.0f);
+    omega[i] = make_float4(ox * c.negGradSpiky, oy * c.negGradSpiky, oz * c.negGradSpiky, 0.0f);
+}
+
+// apply_vorticity.cl:12-86
+__global__ void __launch_bounds__(kBlock)
+apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
+                       const float4* __restrict__ velIn, float4* __restrict__ velOut,
+                       const uint32_t* __restrict__ list, const uint32_t* __restrict__ counts) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = c.n;
+    if (i >= n) return;
+    const float4 pi = pred[i];
+    const uint32_t nd = counts[i] >> 16;
+    float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+    for (uint32_t s = 0; s < nd; ++s) {
+        const uint32_t j = list[(size_t)s * n + i];
+        const float4 pj = pred[j];
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (r2 < c.h2 && fabsf(pj.w) > 1e-8f) {
+            const float rl = sqrtf(r2);
+            const float hr = c.h - rl;
+            const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
+            const float4 oj = omega[j];
+            const float ol = sqrtf(dot3(oj.x, oj.y, oj.z, oj.x, oj.y, oj.z));
+            ex = ex + ol * g0;
+            ey = ey + ol * g1;
+            ez = ez + ol * g2;
+        }
+    }
+    ex = ex * c.negGradSpiky;
+    ey = ey * c.negGradSpiky;
+    ez = ez * c.negGradSpiky;
+    const float l = sqrtf(dot3(ex, ey, ez, ex, ey, ez));
+    if (l > 0.0f) {
+        ex = ex / l;
+        ey = ey / l;
+        ez = ez / l;
+    }
+    const float4 oi = omega[i];
+    const float fx = c.vort * (ey * oi.z - ez * oi.y);
+    const float fy = c.vort * (ez * oi.x - ex * oi.z);
+    const float fz = c.vort * (ex * oi.y - ey * oi.x);
+    const float4 v = velIn[i];
+    velOut[i] = make_float4(v.x + fx * c.dt, v.y + fy * c.dt, v.z + fz * c.dt, v.w + 0.0f);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- launchers --
+void launch_predict_keys(const DevConsts& c, const float4* pos, float4* vel, float4* pred, uint32_t* keys,
+                         uint32_t* perm, int paused, cudaStream_t s) {
+    predict_keys_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pos, vel, pred, keys, perm, paused);
+}
+
+void launch_compute_keys(const DevConsts& c, const float4* pred, uint32_t* keys, uint32_t* perm, cudaStream_t s) {
+    compute_keys_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, keys, perm);
+}
+
+void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, float4* posOut,
+                          float4* predOut, cudaStream_t s) {
+    gather_sorted_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, perm, pos, pred, posOut, predOut);
+}
+
+void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s) {
+    update_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, cells);
+}
+
+void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s) {
+    reset_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, reinterpret_cast<uint2*>(cells));
+}
+
+void launch_build_friends(const DevConsts& c, const float4* pred, const uint32_t* cells, uint32_t* list,
+                          uint32_t* counts, int* errorWord, cudaStream_t s) {
+    build_friends_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, reinterpret_cast<const uint2*>(cells), list,
+                                                            counts, errorWord);
+}
+
+void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
+                            const uint32_t* list, const uint32_t* counts, cudaStream_t s) {
+    compute_scaling_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, predPacked, density, list, counts);
+}
+
+void launch_compute_delta(const DevConsts& c, const float4* predPacked, float4* predOut, const float* density,
+                          const uint32_t* list, const uint32_t* counts, int lastIteration, cudaStream_t s) {
+    compute_delta_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, predPacked, predOut, density, list, counts,
+                                                            lastIteration);
+}
+
+void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
+                              float4* vel, cudaStream_t s) {
+    update_velocities_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, posIn, posOut, vel);
+}
+
+void launch_apply_viscosity(const DevConsts& c, const float4* pred, const float4* velIn, float4* velOut,
+                            float4* omega, const uint32_t* list, const uint32_t* counts, cudaStream_t s) {
+    apply_viscosity_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, velIn, velOut, omega, list, counts);
+}
+
+void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
+                            float4* velOut, const uint32_t* list, const uint32_t* counts, cudaStream_t s) {
+    apply_vorticity_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, omega, velIn, velOut, list, counts);
+}
+
+}  // namespace pbf

@@ -1,0 +1,171 @@
+// pbf_sort.cu — stable LSD radix sort of (cell key, particle index) pairs.
+//
+// The reference sorts with 6 passes of 5 bits over 2048 "virtual processors"
+// (radixsort.cl:61-308, src/Simulation.cpp:456-536).  Its result is the
+// stable sort of the keys (every key is below 2^30), and that order is the
+// contract here: equal keys keep their input order.
+//
+// Here the keys are < gridBufSize, so only ceil(log2(gridBufSize) / 8)
+// passes of 8-bit digits are run (3 at gridBufSize = 2^19).  Each pass is
+//   upsweep   : per-tile 256-bin digit histogram -> hist[digit][tile]
+//   scan      : one exclusive scan over hist in [digit][tile] order
+//   downsweep : per-warp stable ranking with __match_any_sync and per-warp
+//               digit counters in shared memory, then the scatter.
+// A tile is 4096 keys: 8 warps, each owning 512 consecutive keys taken in 16
+// rounds of 32, so (warp, round, lane) order is input order.
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "pbf_internal.h"
+
+namespace pbf {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kRounds = 16;
+constexpr int kTile = kThreads * kRounds;   // 4096 keys
+constexpr int kWarpKeys = 32 * kRounds;     // 512 keys
+constexpr int kScanThreads = 1024;
+
+__global__ void __launch_bounds__(kThreads)
+radix_upsweep_kernel(const uint32_t* __restrict__ keys, int n, int shift, int tiles, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const size_t base = (size_t)blockIdx.x * kTile;
+#pragma unroll 4
+    for (int r = 0; r < kRounds; ++r) {
+        const size_t idx = base + (size_t)r * kThreads + threadIdx.x;
+        if (idx < (size_t)n) atomicAdd(&h[(keys[idx] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of `total` words in place by one block: each thread sums a
+// contiguous chunk, the chunk sums are scanned across the block, and the
+// chunks are rewritten.
+__global__ void __launch_bounds__(kScanThreads)
+radix_scan_kernel(uint32_t* __restrict__ hist, int total) {
+    __shared__ uint32_t warpSums[kScanThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int chunk = (total + kScanThreads - 1) / kScanThreads;
+    const int begin = min(t * chunk, total), end = min(begin + chunk, total);
+    uint32_t sum = 0;
+    for (int k = begin; k < end; ++k) sum += hist[k];
+    // inclusive warp scan of the chunk sums
+    uint32_t incl = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    if (lane == 31) warpSums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warpSums[lane];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, w, d);
+            if (lane >= d) w += v;
+        }
+        warpSums[lane] = w;
+    }
+    __syncthreads();
+    uint32_t run = incl - sum + (warp > 0 ? warpSums[warp - 1] : 0u);
+    for (int k = begin; k < end; ++k) {
+        const uint32_t v = hist[k];
+        hist[k] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+radix_downsweep_kernel(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ permIn,
+                       uint32_t* __restrict__ keysOut, uint32_t* __restrict__ permOut, int n, int shift,
+                       int tiles, const uint32_t* __restrict__ hist) {
+    __shared__ uint32_t warpCount[kWarps][256];
+    __shared__ uint32_t digitBase[256];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) warpCount[w][t] = 0;
+    __syncthreads();
+
+    const size_t base = (size_t)blockIdx.x * kTile + (size_t)warp * kWarpKeys;
+    const unsigned ltMask = (1u << lane) - 1u;
+    uint32_t key[kRounds], rank[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+        const size_t idx = base + (size_t)r * 32 + lane;
+        const bool valid = idx < (size_t)n;
+        const unsigned active = __ballot_sync(0xFFFFFFFFu, valid);
+        uint32_t k = 0, rk = 0, peers = 0, prior = 0;
+        if (valid) {
+            k = keysIn[idx];
+            const uint32_t d = (k >> shift) & 0xFFu;
+            peers = __match_any_sync(active, d);
+            prior = warpCount[warp][d];
+            rk = prior + __popc(peers & ltMask);
+        }
+        __syncwarp();
+        if (valid && (__ffs(peers) - 1) == lane) warpCount[warp][(k >> shift) & 0xFFu] = prior + __popc(peers);
+        __syncwarp();
+        key[r] = k;
+        rank[r] = rk;
+    }
+    __syncthreads();
+    {   // exclusive scan over warps for digit t
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = warpCount[w][t];
+            warpCount[w][t] = run;
+            run += c;
+        }
+        digitBase[t] = hist[(size_t)t * tiles + blockIdx.x];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+        const size_t idx = base + (size_t)r * 32 + lane;
+        if (idx < (size_t)n) {
+            const uint32_t d = (key[r] >> shift) & 0xFFu;
+            const uint32_t dst = digitBase[d] + warpCount[warp][d] + rank[r];
+            keysOut[dst] = key[r];
+            permOut[dst] = permIn[idx];
+        }
+    }
+}
+
+}  // namespace
+
+SortPlan make_sort_plan(int n, uint32_t gridBufSize) {
+    SortPlan p;
+    p.n = n;
+    int bits = 0;
+    while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)gridBufSize) ++bits;  // keys <= gridBufSize-1
+    p.passes = (bits + 7) / 8;
+    p.tiles = (n + kTile - 1) / kTile;
+    p.histWords = (size_t)256 * p.tiles;
+    return p;
+}
+
+int radix_sort_launches(const SortPlan& plan) { return 3 * plan.passes; }
+
+int launch_radix_sort(const SortPlan& plan, uint32_t* keys[2], uint32_t* perm[2], uint32_t* hist,
+                      const float4*, const float4*, float4*, float4*, cudaStream_t s) {
+    int cur = 0;
+    for (int pass = 0; pass < plan.passes; ++pass) {
+        const int shift = 8 * pass;
+        radix_upsweep_kernel<<<plan.tiles, kThreads, 0, s>>>(keys[cur], plan.n, shift, plan.tiles, hist);
+        radix_scan_kernel<<<1, kScanThreads, 0, s>>>(hist, (int)plan.histWords);
+        radix_downsweep_kernel<<<plan.tiles, kThreads, 0, s>>>(keys[cur], perm[cur], keys[cur ^ 1], perm[cur ^ 1],
+                                                               plan.n, shift, plan.tiles, hist);
+        cur ^= 1;
+    }
+    return cur;
+}
+
+}  // namespace pbf

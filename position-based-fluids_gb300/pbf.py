@@ -1,0 +1,354 @@
+"""Python binding of libpbf_gb300.so (ctypes over include/pbf_capi.h).
+
+The class ``Simulation`` keeps the method names of the reference's C++
+``Simulation`` (src/Simulation.hpp:105-128): ``InitBuffers``, ``InitCells``,
+``LoadForceMasks``, ``InitKernels`` and ``Step``; ``load_parameters`` is the
+reference's ``LoadParameters`` (src/ParamUtils.cpp:24-100).  Errors raise
+``PbfError`` with the library's message.  The library must have been built
+(``build.py``); nothing here falls back to another implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_bool, c_char_p, c_float, c_int, c_size_t, c_uint, c_uint32, c_uint64, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libpbf_gb300.so"
+
+PBF_OK = 0
+PBF_ERR_INVALID = -1
+PBF_ERR_CUDA = -2
+PBF_ERR_STATE = -3
+PBF_ERR_UNSUPPORTED = -4
+PBF_ERR_DEVICE_FLAG = -5
+PBF_ERR_NO_DEVICE = -6
+MAX_PARTICLES = 1 << 26
+
+PAD_KEY = 2147483646
+EMPTY = 0xFFFFFFFF
+
+
+class PbfParameters(ctypes.Structure):
+    """Mirror of PbfParameters (include/pbf_params.h); the prefix up to
+    EnableCachedBuffers is the reference's struct Parameters."""
+    _fields_ = [
+        ("resetSimOnChange", c_int), ("particleCount", c_uint),
+        ("xMin", c_float), ("xMax", c_float), ("yMin", c_float), ("yMax", c_float),
+        ("zMin", c_float), ("zMax", c_float),
+        ("waveGenAmp", c_float), ("waveGenFreq", c_float), ("waveGenDuty", c_float),
+        ("timeStep", c_float), ("simIterations", c_uint), ("subSteps", c_uint),
+        ("h", c_float), ("restDensity", c_float), ("epsilon", c_float), ("garvity", c_float),
+        ("vorticityFactor", c_float), ("viscosityFactor", c_float),
+        ("surfaceTenstionK", c_float), ("surfaceTenstionDist", c_float),
+        ("friendsCircles", c_uint), ("particlesPerCircle", c_uint), ("gridBufSize", c_uint),
+        ("setupSpacing", c_float), ("segmentSize", c_uint), ("sortIterations", c_uint),
+        ("particleRenderSize", c_float), ("h_2", c_float), ("EnableCachedBuffers", c_bool),
+        ("gravityVectorEnable", c_int), ("gravityX", c_float), ("gravityY", c_float), ("gravityZ", c_float),
+        ("boxClamp", c_int),
+    ]
+
+    def copy(self) -> "PbfParameters":
+        out = PbfParameters()
+        ctypes.memmove(ctypes.byref(out), ctypes.byref(self), ctypes.sizeof(self))
+        return out
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class PbfError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+_lib = None
+
+
+def library() -> ctypes.CDLL:
+    """Load libpbf_gb300.so; raise when it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise FileNotFoundError(f"{LIB_PATH} is not built; run position-based-fluids_gb300/build.py")
+    lib = ctypes.CDLL(str(LIB_PATH))
+    P = POINTER(PbfParameters)
+    f32p, u32p = POINTER(c_float), POINTER(c_uint32)
+    sig = {
+        "pbf_default_parameters": [P],
+        "pbf_load_parameters": [c_char_p, P, POINTER(c_int)],
+        "pbf_create": [P, c_int, POINTER(c_void_p)],
+        "pbf_destroy": [c_void_p],
+        "pbf_init_buffers": [c_void_p, f32p, f32p],
+        "pbf_init_cells": [c_void_p],
+        "pbf_load_force_masks": [c_void_p, u32p, c_int, c_int],
+        "pbf_init_kernels": [c_void_p],
+        "pbf_set_params": [c_void_p, P],
+        "pbf_set_pause": [c_void_p, c_int],
+        "pbf_step": [c_void_p, c_int],
+        "pbf_step_async": [c_void_p, c_int],
+        "pbf_synchronize": [c_void_p],
+        "pbf_read_state": [c_void_p, c_void_p, c_void_p, c_void_p],
+        "pbf_write_state": [c_void_p, c_void_p, c_void_p],
+        "pbf_device_positions": [c_void_p, POINTER(c_void_p)],
+        "pbf_get_stream": [c_void_p, POINTER(c_void_p)],
+        "pbf_sort_state": [c_void_p, f32p, u32p, u32p, u32p],
+        "pbf_read_friends": [c_void_p, u32p, u32p, c_int],
+        "pbf_enable_stage_timing": [c_void_p, c_int],
+        "pbf_stage_timings": [c_void_p, f32p, c_int, POINTER(c_int), c_char_p, c_size_t],
+        "pbf_launch_count": [c_void_p, POINTER(c_uint64)],
+        "pbf_use_graph": [c_void_p, c_int],
+        "pbf_reference_lattice": [P, f32p],
+        "pbf_scene_block": [c_int, c_int, c_int, c_float, c_float, c_float, c_float, c_float, c_uint64, f32p],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = c_int
+    lib.pbf_last_error.argtypes = [c_void_p]
+    lib.pbf_last_error.restype = c_char_p
+    _lib = lib
+    return lib
+
+
+def _check(rc: int, ctx=None) -> None:
+    if rc != PBF_OK:
+        msg = library().pbf_last_error(ctx).decode(errors="replace")
+        raise PbfError(rc, msg)
+
+
+def _f32(a: np.ndarray):
+    return a.ctypes.data_as(POINTER(c_float))
+
+
+def _u32(a: np.ndarray):
+    return a.ctypes.data_as(POINTER(c_uint32))
+
+
+def default_parameters() -> PbfParameters:
+    p = PbfParameters()
+    _check(library().pbf_default_parameters(ctypes.byref(p)))
+    return p
+
+
+def load_parameters(text: str, base: PbfParameters | None = None) -> PbfParameters:
+    """LoadParameters: parse `.par` text on top of `base` (default: zeros)."""
+    p = base.copy() if base is not None else default_parameters()
+    unknown = c_int(0)
+    _check(library().pbf_load_parameters(text.encode(), ctypes.byref(p), ctypes.byref(unknown)))
+    p._unknown_keys = unknown.value  # type: ignore[attr-defined]
+    return p
+
+
+def load_scenario(name: str) -> PbfParameters:
+    """Load one of the bundled scenario files (scenarios/<name>.par)."""
+    path = PKG / "scenarios" / (name if name.endswith(".par") else name + ".par")
+    return load_parameters(path.read_text())
+
+
+def scene_block(nx: int, ny: int, nz: int, spacing: float, origin=(0.0, 0.0, 0.0), jitter: float = 0.0,
+                seed: int = 0) -> np.ndarray:
+    out = np.zeros((nx * ny * nz, 4), np.float32)
+    _check(library().pbf_scene_block(nx, ny, nz, spacing, float(origin[0]), float(origin[1]), float(origin[2]),
+                                     jitter, seed, _f32(out)))
+    return out
+
+
+def reference_lattice(params: PbfParameters) -> np.ndarray:
+    out = np.zeros((params.particleCount, 4), np.float32)
+    _check(library().pbf_reference_lattice(ctypes.byref(params), _f32(out)))
+    return out
+
+
+class Simulation:
+    """The reference's Simulation over the C-ABI, on one CUDA device."""
+
+    def __init__(self, params: PbfParameters, device: int = 0):
+        self.lib = library()
+        self.params = params.copy()
+        self._ctx = c_void_p()
+        _check(self.lib.pbf_create(ctypes.byref(self.params), device, ctypes.byref(self._ctx)))
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self) -> None:
+        if self._ctx:
+            self.lib.pbf_destroy(self._ctx)
+            self._ctx = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> c_void_p:
+        return self._ctx
+
+    @property
+    def n(self) -> int:
+        return int(self.params.particleCount)
+
+    # -- the reference's methods --------------------------------------------
+    def InitBuffers(self, pos: np.ndarray | None = None, vel: np.ndarray | None = None) -> None:
+        p = None if pos is None else np.ascontiguousarray(pos, np.float32)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        for a in (p, v):
+            if a is not None and a.size != 4 * self.n:
+                raise ValueError("state arrays must hold particleCount float4 records")
+        _check(self.lib.pbf_init_buffers(self._ctx, None if p is None else _f32(p), None if v is None else _f32(v)),
+               self._ctx)
+
+    def InitCells(self) -> None:
+        _check(self.lib.pbf_init_cells(self._ctx), self._ctx)
+
+    def LoadForceMasks(self, mask: np.ndarray | None = None) -> None:
+        if mask is None:
+            _check(self.lib.pbf_load_force_masks(self._ctx, None, 0, 0), self._ctx)
+        else:
+            m = np.ascontiguousarray(mask, np.uint32)
+            _check(self.lib.pbf_load_force_masks(self._ctx, _u32(m), m.shape[1], m.shape[0]), self._ctx)
+
+    def InitKernels(self) -> bool:
+        _check(self.lib.pbf_init_kernels(self._ctx), self._ctx)
+        return True
+
+    def Step(self, substeps: int = 1) -> None:
+        _check(self.lib.pbf_step(self._ctx, substeps), self._ctx)
+
+    @property
+    def bPauseSim(self) -> bool:
+        return bool(getattr(self, "_paused", False))
+
+    @bPauseSim.setter
+    def bPauseSim(self, value: bool) -> None:
+        self._paused = bool(value)
+        _check(self.lib.pbf_set_pause(self._ctx, int(self._paused)), self._ctx)
+
+    # -- conveniences ----------------------------------------------------------
+    @classmethod
+    def create(cls, params: PbfParameters, pos=None, vel=None, device: int = 0) -> "Simulation":
+        """Construct and run InitBuffers, InitCells, LoadForceMasks, InitKernels."""
+        sim = cls(params, device)
+        sim.InitBuffers(pos, vel)
+        sim.InitCells()
+        sim.LoadForceMasks()
+        sim.InitKernels()
+        return sim
+
+    def set_params(self, params: PbfParameters) -> None:
+        _check(self.lib.pbf_set_params(self._ctx, ctypes.byref(params)), self._ctx)
+        self.params = params.copy()
+
+    def step_async(self, substeps: int = 1) -> None:
+        _check(self.lib.pbf_step_async(self._ctx, substeps), self._ctx)
+
+    def synchronize(self) -> None:
+        _check(self.lib.pbf_synchronize(self._ctx), self._ctx)
+
+    def read_state(self):
+        pos = np.empty((self.n, 4), np.float32)
+        vel = np.empty((self.n, 4), np.float32)
+        pred = np.empty((self.n, 4), np.float32)
+        _check(self.lib.pbf_read_state(self._ctx, pos.ctypes.data, vel.ctypes.data, pred.ctypes.data), self._ctx)
+        return pos, vel, pred
+
+    def read_state_into(self, pos_ptr: int | None, vel_ptr: int | None = None, pred_ptr: int | None = None) -> None:
+        _check(self.lib.pbf_read_state(self._ctx, pos_ptr, vel_ptr, pred_ptr), self._ctx)
+
+    def write_state(self, pos: np.ndarray | None = None, vel: np.ndarray | None = None) -> None:
+        p = None if pos is None else np.ascontiguousarray(pos, np.float32)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        _check(self.lib.pbf_write_state(self._ctx, None if p is None else p.ctypes.data,
+                                        None if v is None else v.ctypes.data), self._ctx)
+
+    def write_state_from(self, pos_ptr: int | None, vel_ptr: int | None = None) -> None:
+        _check(self.lib.pbf_write_state(self._ctx, pos_ptr, vel_ptr), self._ctx)
+
+    def sort_state(self, pred: np.ndarray):
+        """Keys, permutation (IntCeil(N, 2048) entries) and cell table from `pred`."""
+        pred = np.ascontiguousarray(pred, np.float32)
+        nkeys = (self.n + 2047) // 2048 * 2048
+        keys = np.empty(nkeys, np.uint32)
+        perm = np.empty(nkeys, np.uint32)
+        cells = np.empty(2 * self.params.gridBufSize, np.uint32)
+        _check(self.lib.pbf_sort_state(self._ctx, _f32(pred), _u32(keys), _u32(perm), _u32(cells)), self._ctx)
+        return keys, perm, cells
+
+    def read_friends(self, slots: int | None = None):
+        """(counts[N,2], list[slots,N]) of the last substep."""
+        if slots is None:
+            slots = int(self.params.friendsCircles * self.params.particlesPerCircle)
+        counts = np.empty((self.n, 2), np.uint32)
+        lst = np.zeros((slots, self.n), np.uint32)
+        _check(self.lib.pbf_read_friends(self._ctx, _u32(counts), _u32(lst), slots), self._ctx)
+        return counts, lst
+
+    def device_positions(self) -> int:
+        p = c_void_p()
+        _check(self.lib.pbf_device_positions(self._ctx, ctypes.byref(p)), self._ctx)
+        return int(p.value or 0)
+
+    def stream(self) -> int:
+        s = c_void_p()
+        _check(self.lib.pbf_get_stream(self._ctx, ctypes.byref(s)), self._ctx)
+        return int(s.value or 0)
+
+    def enable_stage_timing(self, on: bool = True) -> None:
+        _check(self.lib.pbf_enable_stage_timing(self._ctx, int(on)), self._ctx)
+
+    def stage_timings(self) -> dict:
+        ms = (c_float * 64)()
+        count = c_int(0)
+        names = ctypes.create_string_buffer(4096)
+        _check(self.lib.pbf_stage_timings(self._ctx, ms, 64, ctypes.byref(count), names, 4096), self._ctx)
+        keys = names.value.decode().split("\n") if count.value else []
+        return {k: float(ms[i]) for i, k in enumerate(keys)}
+
+    def launch_count(self) -> int:
+        v = c_uint64(0)
+        _check(self.lib.pbf_launch_count(self._ctx, ctypes.byref(v)), self._ctx)
+        return int(v.value)
+
+    def use_graph(self, on: bool) -> None:
+        _check(self.lib.pbf_use_graph(self._ctx, int(on)), self._ctx)
+
+
+EXPORTED_SYMBOLS = sorted(
+    ["pbf_last_error"] + [
+        "pbf_default_parameters", "pbf_load_parameters", "pbf_create", "pbf_destroy", "pbf_init_buffers",
+        "pbf_init_cells", "pbf_load_force_masks", "pbf_init_kernels", "pbf_set_params", "pbf_set_pause",
+        "pbf_step", "pbf_step_async", "pbf_synchronize", "pbf_read_state", "pbf_write_state",
+        "pbf_device_positions", "pbf_get_stream", "pbf_sort_state", "pbf_read_friends",
+        "pbf_enable_stage_timing", "pbf_stage_timings", "pbf_launch_count", "pbf_use_graph",
+        "pbf_reference_lattice", "pbf_scene_block",
+    ])
+
+
+# Dam-break scenes: scenario file + the block the particles start in.
+SCENES = {
+    "dam_break_32k": dict(par="dam_break_32k", block=(32, 32, 32), spacing=0.05, origin=(0.025, 0.025, 0.025),
+                          jitter=0.005, seed=20240601),
+    "dam_break_1m": dict(par="dam_break_1m", block=(128, 64, 128), spacing=0.05, origin=(0.025, 0.025, 0.025),
+                         jitter=0.005, seed=20240601),
+}
+
+
+def make_scene(name: str):
+    """(params, pos[N,4], vel[N,4]) of a bundled dam-break scene."""
+    spec = SCENES[name]
+    params = load_scenario(spec["par"])
+    pos = scene_block(*spec["block"], spec["spacing"], spec["origin"], spec["jitter"], spec["seed"])
+    if pos.shape[0] != params.particleCount:
+        raise ValueError(f"scene {name}: block holds {pos.shape[0]} particles, .par says {params.particleCount}")
+    return params, pos, np.zeros_like(pos)

@@ -1,0 +1,45 @@
+"""The C-ABI library: it loads, exports what include/*.h declares, and fails
+cleanly where no GPU is present (CPU only; no kernel is launched)."""
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+REPO = Path(__file__).resolve().parent.parent
+
+
+def declared_functions() -> set[str]:
+    names = set()
+    for h in (REPO / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names.update(re.findall(r"\b(pbf_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_every_declared_symbol_is_exported(built_lib, pbf_mod):
+    lib = ctypes.CDLL(str(built_lib))
+    declared = declared_functions()
+    assert declared, "no declarations found"
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, f"declared but not exported: {missing}"
+    assert set(pbf_mod.EXPORTED_SYMBOLS) <= declared
+
+
+def test_create_without_device_or_with_bad_args(pbf_mod):
+    from tests.conftest import has_cuda_device
+    p = pbf_mod.load_scenario("dam_break_32k")
+    if not has_cuda_device():
+        with pytest.raises(pbf_mod.PbfError) as e:
+            pbf_mod.Simulation(p)
+        assert e.value.code == pbf_mod.PBF_ERR_NO_DEVICE
+    lib = pbf_mod.library()
+    ctx = ctypes.c_void_p()
+    assert lib.pbf_create(None, 0, ctypes.byref(ctx)) == pbf_mod.PBF_ERR_INVALID
+    assert b"NULL" in lib.pbf_last_error(None)
+    # calls on a NULL context are rejected, not crashed
+    assert lib.pbf_step(None, 1) == pbf_mod.PBF_ERR_INVALID
+    assert lib.pbf_init_cells(None) == pbf_mod.PBF_ERR_INVALID
+    assert lib.pbf_destroy(None) == pbf_mod.PBF_OK

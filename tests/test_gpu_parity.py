@@ -1,0 +1,254 @@
+"""The CUDA path against the oracle, through the C-ABI (needs a GPU).
+
+Contract: the sort permutation, keys and cell table are bit-exact; one and
+many substeps of positions, velocities and predictions are bit-exact as
+well (NaN payloads aside: every NaN is compared as NaN).  The tolerance the
+path promises is 1e-5 relative (max |gpu - oracle| / max |oracle| per array),
+which bit-exact results meet trivially; the relative error is computed and
+checked as well so a regression reports a figure, not only a mismatch.
+"""
+from __future__ import annotations
+
+import hashlib
+import importlib.util
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+REL_TOL = 1e-5
+
+
+def _mg():
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+MG = None
+
+
+def mg():
+    global MG
+    if MG is None:
+        MG = _mg()
+    return MG
+
+
+def assert_same(name, got, want):
+    g, w = mg().canonical(got), mg().canonical(want)
+    same = np.array_equal(g.view(np.uint32), w.view(np.uint32))
+    if not same:
+        finite = np.isfinite(w) & np.isfinite(g)
+        scale = float(np.max(np.abs(w[finite]))) if finite.any() else 1.0
+        rel = float(np.max(np.abs(g[finite] - w[finite]))) / max(scale, 1e-30) if finite.any() else np.inf
+        nbad = int(np.sum(g.view(np.uint32) != w.view(np.uint32)))
+        nan_mismatch = int(np.sum(np.isnan(g) != np.isnan(w)))
+        raise AssertionError(f"{name}: {nbad} words differ (rel err {rel:.3e}, NaN mismatches {nan_mismatch})")
+
+
+def run_gpu(pbf, params, pos, vel, substeps, device, graph=True, friends=True):
+    with pbf.Simulation.create(params, pos, vel, device=device) as sim:
+        sim.use_graph(graph)
+        sim.Step(substeps)
+        p, v, pr = sim.read_state()
+        counts, lst = sim.read_friends() if friends else (None, None)
+    return p, v, pr, counts, lst
+
+
+def scene(pbf, dims, base="dam_break_32k", spacing=0.05, origin=(0.025,) * 3, jitter=0.005, seed=20240601, **ov):
+    params = pbf.load_scenario(base)
+    for k, v in ov.items():
+        setattr(params, k, v)
+    params.particleCount = dims[0] * dims[1] * dims[2]
+    pos = pbf.scene_block(*dims, spacing, origin, jitter, seed)
+    return params, pos, np.zeros_like(pos)
+
+
+# ------------------------------------------------------------------ sort --
+@pytest.mark.parametrize("case", [
+    dict(dims=(32, 32, 32)),
+    dict(dims=(17, 13, 11)),                      # N not a multiple of 32 / 2048
+    dict(dims=(16, 16, 16), gridBufSize=64),      # hash collisions
+    dict(dims=(16, 16, 16), gridBufSize=1000),    # modulo, not a power of two
+    dict(dims=(2, 1, 1)),                         # two particles
+])
+def test_sort_and_cells_bit_exact(case, pbf_mod, oracle_mod, cuda_device):
+    case = dict(case)
+    dims = case.pop("dims")
+    params, pos, vel = scene(pbf_mod, dims, **case)
+    rng = np.random.default_rng(3)
+    pred = pos.copy()
+    pred[:, :3] += rng.uniform(-0.02, 0.02, (len(pos), 3)).astype(np.float32)
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        gk, gp, gc = sim.sort_state(pred)
+    ok, op, oc = oracle_mod.sort(params, pred)
+    assert np.array_equal(gk, ok), "keys"
+    assert np.array_equal(gp, op), "permutation"
+    assert np.array_equal(gc, oc), "cell table"
+
+
+def test_sort_at_full_scale_properties(pbf_mod, oracle_mod, cuda_device):
+    """1M particles: bit-exact against the oracle, plus the properties of a
+    stable sort (sorted keys, a permutation, stable ties)."""
+    params, pos, vel = pbf_mod.make_scene("dam_break_1m")
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        gk, gp, gc = sim.sort_state(pos)
+    n = len(pos)
+    assert np.all(np.diff(gk[:n].astype(np.int64)) >= 0)
+    assert np.array_equal(np.sort(gp[:n]), np.arange(n, dtype=np.uint32))
+    same = gk[1:n] == gk[:n - 1]
+    assert np.all(gp[1:n][same] > gp[:n - 1][same]), "ties keep input order"
+    ok, op, oc = oracle_mod.sort(params, pos)
+    assert np.array_equal(gk, ok) and np.array_equal(gp, op) and np.array_equal(gc, oc)
+
+
+# -------------------------------------------------------- golden digests --
+MANIFEST = json.loads((GOLDEN / "golden.json").read_text())
+
+
+@pytest.mark.parametrize("case", MANIFEST["cases"], ids=[c["name"] for c in MANIFEST["cases"]])
+def test_gpu_matches_reference_kernel_digests(case, pbf_mod, cuda_device):
+    """Outputs of the reference's own kernels (tests/golden) reproduced on the GPU."""
+    params, pos, vel = mg().scene(tuple(case["block"]), case["overrides"])
+    p, v, pr, _, _ = run_gpu(pbf_mod, params, pos, vel, case["substeps"], cuda_device, friends=False)
+    for name, arr in (("pos", p), ("vel", v), ("pred", pr)):
+        assert mg().digest(arr) == case["sha256"][name], f"{case['name']}: {name}"
+
+
+# ------------------------------------------------------- substep parity --
+SUBSTEP_CASES = {
+    "dam32k_clamped_1": (dict(dims=(32, 32, 32)), 1),
+    "dam32k_clamped_4": (dict(dims=(32, 32, 32)), 4),
+    "literal_clamped_6": (dict(dims=(24, 24, 24), base="dam_break_32k_literal"), 6),
+    "gravity_vector": (dict(dims=(20, 16, 12), gravityVectorEnable=1, gravityX=1.2, gravityY=-9.0, gravityZ=0.5), 3),
+    "zero_iterations": (dict(dims=(16, 16, 16), simIterations=0), 2),
+    "one_iteration_odd": (dict(dims=(19, 7, 23), simIterations=1), 2),
+    "collisions_clamped": (dict(dims=(16, 16, 16), gridBufSize=128), 2),
+    "two_particles": (dict(dims=(2, 1, 1)), 3),
+    "one_particle": (dict(dims=(1, 1, 1)), 2),
+}
+
+
+@pytest.mark.parametrize("name", list(SUBSTEP_CASES))
+def test_substeps_bit_exact(name, pbf_mod, oracle_mod, cuda_device):
+    spec, substeps = SUBSTEP_CASES[name]
+    spec = dict(spec)
+    dims = spec.pop("dims")
+    params, pos, vel = scene(pbf_mod, dims, **spec)
+    gp, gv, gpr, gcounts, glist = run_gpu(pbf_mod, params, pos, vel, substeps, cuda_device)
+    op, ov, opr, dbg = oracle_mod.step(params, pos, vel, substeps, debug=True)
+    assert np.array_equal(gcounts, dbg["counts"]), "friend counts"
+    slots = int(dbg["counts"][:, 0].max()) if len(dbg["counts"]) else 0
+    for s in range(slots):
+        used = dbg["counts"][:, 0] > s
+        assert np.array_equal(glist[s][used], dbg["list"][s][used]), f"friend list slot {s}"
+    assert_same("pos", gp, op)
+    assert_same("vel", gv, ov)
+    assert_same("pred", gpr, opr)
+
+
+def test_graph_and_eager_paths_agree(pbf_mod, cuda_device):
+    params, pos, vel = scene(pbf_mod, (20, 20, 20))
+    a = run_gpu(pbf_mod, params, pos, vel, 5, cuda_device, graph=True)
+    b = run_gpu(pbf_mod, params, pos, vel, 5, cuda_device, graph=False)
+    for name, x, y in zip(("pos", "vel", "pred"), a[:3], b[:3]):
+        assert_same(name, x, y)
+
+
+def test_paused_steps_match_oracle(pbf_mod, oracle_mod, cuda_device):
+    """bPauseSim: no gravity, no sort; the previous sorted keys are reused."""
+    params, pos, vel = scene(pbf_mod, (16, 16, 12))
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        sim.Step(2)
+        sim.bPauseSim = True
+        sim.Step(2)
+        sim.bPauseSim = False
+        sim.Step(1)
+        gp, gv, gpr = sim.read_state()
+    keys = np.zeros(oracle_mod.n_keys(len(pos)), np.uint32)
+    p, v, _ = oracle_mod.step(params, pos, vel, 2, keys_state=keys)
+    p, v, _ = oracle_mod.step(params, p, v, 2, paused=True, keys_state=keys)
+    p, v, pr = oracle_mod.step(params, p, v, 1, keys_state=keys)
+    assert_same("pos", gp, p)
+    assert_same("vel", gv, v)
+    assert_same("pred", gpr, pr)
+
+
+def test_rollout_300_frames_bit_exact(pbf_mod, oracle_mod, cuda_device):
+    """The 32,768-particle dam break for 300 frames (600 substeps): identical
+    to the oracle at every checkpoint, with density error and energy stated."""
+    params, pos, vel = pbf_mod.make_scene("dam_break_32k")
+    checkpoints = [2, 20, 200, 600]
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        op, ov = pos, vel
+        done = 0
+        for cp in checkpoints:
+            sim.Step(cp - done)
+            op, ov, opr = oracle_mod.step(params, op, ov, cp - done)
+            done = cp
+            gp, gv, gpr = sim.read_state()
+            assert_same(f"pos@{cp}", gp, op)
+            assert_same(f"vel@{cp}", gv, ov)
+            assert_same(f"pred@{cp}", gpr, opr)
+            rho = gpr[:, 3]
+            ok = np.isfinite(rho)
+            err = np.abs(rho[ok] / params.restDensity - 1.0)
+            ke = 0.5 * np.sum(gv[ok, :3].astype(np.float64) ** 2)
+            pe = params.garvity * np.sum(gp[ok, 1].astype(np.float64))
+            print(f"substep {cp}: density error mean {err.mean():.4f} max {err.max():.3f}; "
+                  f"kinetic {ke:.2f} potential {pe:.2f}; non-finite {int((~ok).sum())}")
+
+
+def test_one_substep_at_1m_bit_exact_and_fp64_error(pbf_mod, oracle_mod, cuda_device):
+    """1,048,576 particles: one substep bit-exact against the FP32 oracle; the
+    max error against the FP64 oracle is stated."""
+    params, pos, vel = pbf_mod.make_scene("dam_break_1m")
+    gp, gv, gpr, _, _ = run_gpu(pbf_mod, params, pos, vel, 1, cuda_device, friends=False)
+    op, ov, opr = oracle_mod.step(params, pos, vel, 1)
+    assert_same("pos", gp, op)
+    assert_same("vel", gv, ov)
+    assert_same("pred", gpr, opr)
+    dp, dv, _ = oracle_mod.step_f64(params, pos, vel, 1)
+    for name, g, d in (("pos", gp, dp), ("vel", gv, dv)):
+        err = np.abs(g[:, :3].astype(np.float64) - d[:, :3])
+        rel = err.max() / np.abs(d[:, :3]).max()
+        print(f"1M, one substep, {name}: max |fp32 - fp64| = {err.max():.3e} (relative {rel:.3e})")
+
+
+def test_stage_timings_and_launch_count(pbf_mod, cuda_device):
+    params, pos, vel = scene(pbf_mod, (16, 16, 16))
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        sim.enable_stage_timing(True)
+        sim.Step(1)
+        t = sim.stage_timings()
+        for name in ("predictPositions", "radixsort", "sortParticles", "updateCells", "buildFriendsList",
+                     "computeScaling", "computeDelta", "updateVelocities", "applyViscosity", "applyVorticity"):
+            assert name in t and t[name] >= 0.0
+        assert sim.launch_count() > 0
+
+
+def test_argument_errors(pbf_mod, cuda_device):
+    params, pos, vel = scene(pbf_mod, (8, 8, 8))
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        bad = params.copy()
+        bad.particleCount = 999
+        with pytest.raises(pbf_mod.PbfError):
+            sim.set_params(bad)
+        bad = params.copy()
+        bad.friendsCircles = 9
+        with pytest.raises(pbf_mod.PbfError):
+            sim.set_params(bad)
+        with pytest.raises(pbf_mod.PbfError) as e:
+            sim.LoadForceMasks(np.ones((4, 4), np.uint32))
+        assert e.value.code == pbf_mod.PBF_ERR_UNSUPPORTED
+    s = pbf_mod.Simulation(params, cuda_device)
+    with pytest.raises(pbf_mod.PbfError) as e:
+        s.Step(1)
+    assert e.value.code == pbf_mod.PBF_ERR_STATE
+    s.close()

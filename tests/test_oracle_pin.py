@@ -1,0 +1,125 @@
+"""The oracle against the reference's own kernels (CPU only).
+
+The reference ships no tests or golden data, so the oracle is pinned against
+the reference's kernel sources themselves: tests/golden/ holds digests of
+their outputs (generated by tests/golden/make_golden.py through
+oracle/clshim.hpp), and where the reference checkout is present the oracle is
+also run side by side with the shimmed kernels on fresh cases.
+"""
+from __future__ import annotations
+
+import hashlib
+import importlib.util
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def _make_golden():
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _digest(a):
+    return _make_golden().digest(a)
+
+
+MANIFEST = json.loads((GOLDEN / "golden.json").read_text())
+
+
+@pytest.mark.parametrize("case", MANIFEST["cases"], ids=[c["name"] for c in MANIFEST["cases"]])
+def test_oracle_matches_reference_digests(case, pbf_mod, oracle_mod):
+    mg = _make_golden()
+    params, pos, vel = mg.scene(tuple(case["block"]), case["overrides"])
+    p, v, pr, dbg = oracle_mod.step(params, pos, vel, case["substeps"], debug=True)
+    got = {"pos": p, "vel": v, "pred": pr, "keys": dbg["keys"], "perm": dbg["perm"], "cells": dbg["cells"]}
+    for k, want in case["sha256"].items():
+        assert _digest(got[k]) == want, f"{case['name']}: {k} differs from the reference kernels"
+
+
+def test_oracle_matches_small_case_arrays(pbf_mod, oracle_mod):
+    data = np.load(GOLDEN / "small_case.npz")
+    mg = _make_golden()
+    case = next(c for c in MANIFEST["cases"] if c["name"] == "small_2k_2sub")
+    params, pos, vel = mg.scene(tuple(case["block"]), case["overrides"])
+    assert np.array_equal(pos, data["init_pos"])
+    p, v, pr = oracle_mod.step(params, pos, vel, case["substeps"])
+    for name, arr in (("pos", p), ("vel", v), ("pred", pr)):
+        assert np.array_equal(arr.view(np.uint32), data[name].view(np.uint32)), name
+
+
+def test_sort_is_stable_argsort(pbf_mod, oracle_mod):
+    """The 6-pass, 5-bit reference sort equals a stable sort by key."""
+    params = pbf_mod.load_scenario("dam_break_32k")
+    rng = np.random.default_rng(5)
+    n = 5000
+    params.particleCount = n
+    pred = np.zeros((n, 4), np.float32)
+    pred[:, :3] = rng.uniform(0.0, 1.6, (n, 3)).astype(np.float32)
+    keys, perm, cells = oracle_mod.sort(params, pred)
+    raw = np.array([oracle_mod.grid_hash(int(x), int(y), int(z), params.gridBufSize)
+                    for x, y, z in (pred[:, :3] / np.float32(params.h)).astype(np.int32)], np.uint32)
+    order = np.argsort(raw, kind="stable")
+    nk = oracle_mod.n_keys(n)
+    assert np.array_equal(perm[:n], order)
+    assert np.array_equal(keys[:n], raw[order])
+    assert np.all(keys[n:] == 2147483646) and np.array_equal(perm[n:], np.arange(n, nk))
+    # cell table: start/end (inclusive) of every occupied key, all ones elsewhere
+    table = cells.reshape(-1, 2)
+    occupied = np.unique(raw)
+    for k in occupied[:200]:
+        idx = np.nonzero(keys[:n] == k)[0]
+        assert table[k, 0] == idx[0] and table[k, 1] == idx[-1]
+    empty = np.setdiff1d(np.arange(params.gridBufSize), occupied)
+    assert np.all(table[empty] == 0xFFFFFFFF)
+
+
+needs_ref = pytest.mark.skipif(
+    not __import__("oracle.oracle", fromlist=["ref_available"]).ref_available(),
+    reason="the reference kernels are not available here")
+
+
+@needs_ref
+@pytest.mark.parametrize("seed,substeps,overrides", [
+    (1, 3, {}),
+    (2, 2, {"viscosityFactor": 0.05, "vorticityFactor": 0.01, "surfaceTenstionK": -0.3}),
+    (3, 2, {"epsilon": 100.0, "restDensity": 5000.0}),
+    (4, 1, {"gridBufSize": 1000}),  # not a power of two: the modulo path
+])
+def test_oracle_matches_reference_live(seed, substeps, overrides, pbf_mod, oracle_mod):
+    params = pbf_mod.load_scenario("dam_break_32k")
+    params.boxClamp = 0
+    for k, v in overrides.items():
+        setattr(params, k, v)
+    dims = (12, 20, 9)
+    n = dims[0] * dims[1] * dims[2]
+    params.particleCount = n
+    pos = pbf_mod.scene_block(*dims, 0.05, (0.3, 0.2, 0.1), 0.01, seed)
+    rng = np.random.default_rng(seed)
+    vel = np.zeros_like(pos)
+    vel[:, :3] = rng.normal(0, 0.2, (n, 3)).astype(np.float32)
+    a = oracle_mod.step(params, pos, vel, substeps)
+    b = oracle_mod.ref_step(params, pos, vel, substeps)
+    mg = _make_golden()
+    for x, y, name in zip(a, b[:3], ("pos", "vel", "pred")):
+        assert np.array_equal(mg.canonical(x).view(np.uint32), mg.canonical(y).view(np.uint32)), name
+
+
+def test_fp64_oracle_close_to_fp32(pbf_mod, oracle_mod):
+    """The FP64 oracle runs the same pipeline; one substep stays close."""
+    params = pbf_mod.load_scenario("dam_break_32k")
+    dims = (16, 16, 16)
+    params.particleCount = 4096
+    params.boxClamp = 0
+    pos = pbf_mod.scene_block(*dims, 0.05, (0.025,) * 3, 0.005, 7)
+    vel = np.zeros_like(pos)
+    p32, v32, _ = oracle_mod.step(params, pos, vel, 1)
+    p64, v64, _ = oracle_mod.step_f64(params, pos, vel, 1)
+    assert np.max(np.abs(p32[:, :3] - p64[:, :3])) < 1e-5
+    assert np.max(np.abs(v32[:, :3] - v64[:, :3])) < 5e-3
