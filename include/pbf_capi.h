@@ -54,8 +54,8 @@ int pbf_default_parameters(PbfParameters* out);
    line, `#` starts a comment, keys case-insensitive, unknown keys reported on
    stderr and ignored, and a final line with no trailing newline is dropped
    with "Error parsing parameters file".  Extra keys accepted here:
-   gravityx / gravityy / gravityz (any of them enables the gravity vector) and
-   boxclamp.  Returns the number of unknown keys through *unknown (may be NULL). */
+   gravityx / gravityy / gravityz (any of them enables the gravity vector),
+   boxclamp and zerodistanceguard.  Returns the number of unknown keys through *unknown (may be NULL). */
 int pbf_load_parameters(const char* text, PbfParameters* inout, int* unknown);
 
 /* -------------------------------------------------------------- lifetime -- */

@@ -65,6 +65,11 @@ typedef struct PbfParameters {
        the delta-p stage, after the position update is formed and before the
        delta is taken.  0: no clamp (the reference's behaviour). */
     int          boxClamp;
+    /* 1: a neighbour at distance exactly 0 contributes nothing to the density,
+       delta-p, viscosity and vorticity sums.  0: it is summed as in the
+       reference, where r / |r| is 0/0 and the particle's state becomes NaN
+       (compute_scaling.cl:76-83, compute_delta.cl:142-146). */
+    int          zeroDistanceGuard;
 } PbfParameters;
 
 /* Largest friend-circle configuration the kernels accept. */

@@ -23,7 +23,9 @@
 // racy or silent: applyViscosity reads the pre-pass velocities of every
 // neighbour (Jacobi; the reference updates in place while neighbours read,
 // apply_viscosity.cl:46,81), and an optional box clamp is applied to the
-// updated position in computeDelta before the delta is taken.
+// updated position in computeDelta before the delta is taken.  With the
+// optional zero-distance guard a neighbour at distance exactly 0 is left out
+// of the four solver sums (the reference divides 0 by 0 there).
 //
 // Templated on the scalar type: float is the parity oracle, double is the
 // FP64 oracle used to state error bounds.
@@ -94,7 +96,7 @@ const uint32_t kPadKey = 2147483647u - 1u;     // radixsort.cl:17
 template <typename T> struct Consts {
     T dt, h, h2, minR, hMinusMinR, poly6, gradSpiky, poly6q, rho0, eps, K, visc, vort;
     T gx, gy, gz, lo[3], hi[3];
-    int clamp;
+    int clamp, guard;
     int circles, perCircle;
     uint32_t grid;
 };
@@ -120,6 +122,7 @@ template <typename T> Consts<T> make_consts(const PbfParameters& p) {
     c.lo[0] = p.xMin; c.lo[1] = p.yMin; c.lo[2] = p.zMin;
     c.hi[0] = p.xMax; c.hi[1] = p.yMax; c.hi[2] = p.zMax;
     c.clamp = p.boxClamp;
+    c.guard = p.zeroDistanceGuard;
     c.circles = (int)p.friendsCircles; c.perCircle = (int)p.particlesPerCircle;
     c.grid = p.gridBufSize;
     return c;
@@ -299,7 +302,7 @@ template <typename T> void compute_scaling(State<T>& s, const Consts<T>& c) {
             for (int f = 0; f < cnt[k]; ++f) {
                 V3<T> r = sub(pi, xyz(s.pred[lst[k * P + f]]));
                 T r2 = dot(r, r);
-                if (r2 < c.h2) {
+                if (r2 < c.h2 && (!c.guard || r2 > (T)0)) {
                     T rl = std::sqrt(r2);
                     T hr = c.h - rl;
                     T sc = c.gradSpiky * hr * hr;
@@ -338,7 +341,7 @@ template <typename T> void compute_delta(State<T>& s, const Consts<T>& c) {
                 V4<T> pj = s.predP[lst[k * P + f]];
                 V3<T> r = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
                 T r2 = dot(r, r);
-                if (r2 < c.h2) {
+                if (r2 < c.h2 && (!c.guard || r2 > (T)0)) {
                     T rl = std::sqrt(r2);
                     T hr = c.h - rl;
                     V3<T> g = {(r.x / rl) * hr * hr, (r.y / rl) * hr * hr, (r.z / rl) * hr * hr};
@@ -394,7 +397,7 @@ template <typename T> void apply_viscosity(State<T>& s, const Consts<T>& c) {
                 V4<T> pj = s.pred[j], vj = vold[j];
                 V3<T> r = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
                 T r2 = r.x * r.x + r.y * r.y + r.z * r.z;
-                if (r2 < c.h2) {
+                if (r2 < c.h2 && (!c.guard || r2 > (T)0)) {
                     if (std::fabs(pj.w) > (T)1e-8f) {
                         V3<T> v = {vj.x - vi.x, vj.y - vi.y, vj.z - vi.z};
                         T d = c.h2 - r2;
@@ -430,7 +433,7 @@ template <typename T> void apply_vorticity(State<T>& s, const Consts<T>& c) {
                 V4<T> pj = s.pred[j];
                 V3<T> r = {pi.x - pj.x, pi.y - pj.y, pi.z - pj.z};
                 T r2 = r.x * r.x + r.y * r.y + r.z * r.z;
-                if (r2 < c.h2) {
+                if (r2 < c.h2 && (!c.guard || r2 > (T)0)) {
                     if (std::fabs(pj.w) > (T)1e-8f) {
                         T rl = std::sqrt(r2);
                         T hr = c.h - rl;

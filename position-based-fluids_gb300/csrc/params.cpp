@@ -86,6 +86,7 @@ extern "C" int pbf_load_parameters(const char* text, PbfParameters* p, int* unkn
         else if (key == "gravityy") { fields >> p->gravityY; p->gravityVectorEnable = 1; }
         else if (key == "gravityz") { fields >> p->gravityZ; p->gravityVectorEnable = 1; }
         else if (key == "boxclamp") fields >> p->boxClamp;
+        else if (key == "zerodistanceguard") fields >> p->zeroDistanceGuard;
         else {
             std::cerr << "Unknown parameter " << key << std::endl << "Leaving it out." << std::endl;
             ++nUnknown;

@@ -47,7 +47,7 @@ struct pbf_ctx {
     uint32_t* hist = nullptr;
     uint32_t* cells = nullptr;
     uint32_t* list = nullptr;
-    uint32_t* counts = nullptr;
+    uint2* meta = nullptr;       // per-particle friend counts per circle + kept circles
     int* errWord = nullptr;
     size_t histWords = 0;
     uint32_t cellsWords = 0;  // gridBufSize the cell table was allocated for
@@ -115,6 +115,7 @@ DevConsts make_consts(const PbfParameters& p, int n) {
     c.lo[0] = p.xMin; c.lo[1] = p.yMin; c.lo[2] = p.zMin;
     c.hi[0] = p.xMax; c.hi[1] = p.yMax; c.hi[2] = p.zMax;
     c.clamp = p.boxClamp ? 1 : 0;
+    c.guard = p.zeroDistanceGuard ? 1 : 0;
     c.circles = (int)p.friendsCircles;
     c.perCircle = (int)p.particlesPerCircle;
     c.grid = p.gridBufSize;
@@ -237,7 +238,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
     mark("updateCells");
     pbf::launch_update_cells(c.n, keys, ctx->cells, s);
     mark("buildFriendsList");
-    pbf::launch_build_friends(c, ctx->pred[sortedPred], ctx->cells, ctx->list, ctx->counts, ctx->errWord, s);
+    pbf::launch_build_friends(c, ctx->pred[sortedPred], ctx->cells, ctx->list, ctx->meta, ctx->errWord, s);
     mark("resetPartList");
     pbf::launch_reset_cells(c.n, keys, ctx->cells, s);
     launched += 3;
@@ -245,9 +246,9 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
     const unsigned iters = ctx->params.simIterations;
     for (unsigned it = 0; it < iters; ++it) {
         mark("computeScaling");
-        pbf::launch_compute_scaling(c, ctx->pred[a], ctx->pred[a ^ 1], ctx->density, ctx->list, ctx->counts, s);
+        pbf::launch_compute_scaling(c, ctx->pred[a], ctx->pred[a ^ 1], ctx->density, ctx->list, ctx->meta, s);
         mark("computeDelta");
-        pbf::launch_compute_delta(c, ctx->pred[a ^ 1], ctx->pred[a], ctx->density, ctx->list, ctx->counts,
+        pbf::launch_compute_delta(c, ctx->pred[a ^ 1], ctx->pred[a], ctx->density, ctx->list, ctx->meta,
                                   it + 1 == iters, s);
         launched += 2;
     }
@@ -259,9 +260,9 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
     mark("updateVelocities");
     pbf::launch_update_velocities(c, ctx->pred[a], ctx->pos[sortedPos], ctx->pos[sortedPos ^ 1], ctx->vel[V], s);
     mark("applyViscosity");
-    pbf::launch_apply_viscosity(c, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], ctx->omega, ctx->list, ctx->counts, s);
+    pbf::launch_apply_viscosity(c, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], ctx->omega, ctx->list, ctx->meta, s);
     mark("applyVorticity");
-    pbf::launch_apply_vorticity(c, ctx->pred[a], ctx->omega, ctx->vel[V ^ 1], ctx->vel[V], ctx->list, ctx->counts, s);
+    pbf::launch_apply_vorticity(c, ctx->pred[a], ctx->omega, ctx->vel[V ^ 1], ctx->vel[V], ctx->list, ctx->meta, s);
     launched += 3;
     PBF_CUDA(ctx, cudaGetLastError());
     ctx->curPos = sortedPos ^ 1;
@@ -350,7 +351,7 @@ int pbf_destroy(pbf_ctx* ctx) {
         dev_free(ctx->keys[k]); dev_free(ctx->perm[k]);
     }
     dev_free(ctx->omega); dev_free(ctx->density); dev_free(ctx->hist); dev_free(ctx->cells);
-    dev_free(ctx->list); dev_free(ctx->counts); dev_free(ctx->errWord);
+    dev_free(ctx->list); dev_free(ctx->meta); dev_free(ctx->errWord);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PBF_OK;
@@ -411,9 +412,9 @@ int pbf_init_cells(pbf_ctx* ctx) {
     PBF_CUDA(ctx, cudaMemset(ctx->cells, 0xFF, 8 * (size_t)p.gridBufSize));
     ctx->cellsWords = p.gridBufSize;
     ctx->listSlots = (int)(p.friendsCircles * p.particlesPerCircle);
-    if ((rc = dev_alloc(ctx, &ctx->list, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->counts, ctx->n)))
+    if ((rc = dev_alloc(ctx, &ctx->list, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->meta, ctx->n)))
         return rc;
-    PBF_CUDA(ctx, cudaMemset(ctx->counts, 0, 4 * (size_t)ctx->n));
+    PBF_CUDA(ctx, cudaMemset(ctx->meta, 0, 8 * (size_t)ctx->n));
     ctx->cellsReady = true;
     ctx->kernelsReady = false;
     return PBF_OK;
@@ -597,17 +598,28 @@ int pbf_read_friends(pbf_ctx* ctx, uint32_t* counts, uint32_t* list, int list_sl
     if (rc) return rc;
     if (!ctx->stepped) return fail(ctx, PBF_ERR_STATE, "no substep has run yet");
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
-    const int n = ctx->n;
-    if (counts) {
-        std::vector<uint32_t> packed(n);
-        PBF_CUDA(ctx, cudaMemcpyAsync(packed.data(), ctx->counts, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
-        PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        for (int i = 0; i < n; ++i) { counts[2 * i] = packed[i] & 0xFFFFu; counts[2 * i + 1] = packed[i] >> 16; }
-    }
+    const int n = ctx->n, P = (int)ctx->params.particlesPerCircle;
+    std::vector<uint2> meta(n);
+    PBF_CUDA(ctx, cudaMemcpyAsync(meta.data(), ctx->meta, 8 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<uint32_t> rows;
     if (list && list_slots > 0) {
-        const int slots = std::min(list_slots, ctx->listSlots);
-        PBF_CUDA(ctx, cudaMemcpyAsync(list, ctx->list, 4 * (size_t)slots * n, cudaMemcpyDeviceToHost, ctx->stream));
-        PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        rows.resize((size_t)ctx->listSlots * n);
+        PBF_CUDA(ctx, cudaMemcpyAsync(rows.data(), ctx->list, 4 * rows.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < n; ++i) {
+        const uint64_t m = (uint64_t)meta[i].x | ((uint64_t)meta[i].y << 32);
+        const int keptL = (int)(m >> 56) & 0xF, keptD = (int)(m >> 60) & 0xF;
+        uint32_t nl = 0, nd = 0, slot = 0;
+        for (int k = 0; k < keptL; ++k) {
+            const uint32_t cnt = (uint32_t)(m >> (7 * k)) & 0x7Fu;
+            nl += cnt;
+            if (k < keptD) nd += cnt;
+            if (!rows.empty())
+                for (uint32_t f = 0; f < cnt; ++f, ++slot)
+                    if ((int)slot < list_slots) list[(size_t)slot * n + i] = rows[(size_t)(k * P + (int)f) * n + i];
+        }
+        if (counts) { counts[2 * i] = nl; counts[2 * i + 1] = nd; }
     }
     return PBF_OK;
 }

@@ -19,7 +19,7 @@ struct DevConsts {
     float rho0, rho0sq, eps, K, visc, vort;
     float gx, gy, gz;
     float lo[3], hi[3];
-    int clamp;
+    int clamp, guard;
     int circles, perCircle;
     uint32_t grid;
     int n;
@@ -40,17 +40,17 @@ void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const 
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
 void launch_build_friends(const DevConsts& c, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint32_t* counts, int* errorWord, cudaStream_t s);
+                          uint2* meta, int* errorWord, cudaStream_t s);
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
-                            const uint32_t* list, const uint32_t* counts, cudaStream_t s);
+                            const uint32_t* list, const uint2* meta, cudaStream_t s);
 void launch_compute_delta(const DevConsts& c, const float4* predPacked, float4* predOut, const float* density,
-                          const uint32_t* list, const uint32_t* counts, int lastIteration, cudaStream_t s);
+                          const uint32_t* list, const uint2* meta, int lastIteration, cudaStream_t s);
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
                               float4* vel, cudaStream_t s);
 void launch_apply_viscosity(const DevConsts& c, const float4* pred, const float4* velIn, float4* velOut,
-                            float4* omega, const uint32_t* list, const uint32_t* counts, cudaStream_t s);
+                            float4* omega, const uint32_t* list, const uint2* meta, cudaStream_t s);
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
-                            float4* velOut, const uint32_t* list, const uint32_t* counts, cudaStream_t s);
+                            float4* velOut, const uint32_t* list, const uint2* meta, cudaStream_t s);
 
 // ---- radix sort (pbf_sort.cu) ----
 struct SortPlan {

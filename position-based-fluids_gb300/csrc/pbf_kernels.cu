@@ -14,11 +14,15 @@
 //   pos, pred, vel, omega : float4[N]  (16-byte records, coalesced 128-bit I/O)
 //   keys, perm            : uint32[N]
 //   cells                 : uint2[gridBufSize]  (start, inclusive end)
-//   counts                : uint32[N]   low 16 bits: neighbours used by the
-//                           density pass, high 16 bits: by the delta,
-//                           viscosity and vorticity passes
-//   list                  : uint32[slots][N]  slot-major, so that a warp of
-//                           consecutive particles reads one slot coalesced.
+//   list                  : uint32[circles * perCircle][N]: friend s of circle
+//                           c of particle i at row c*perCircle + s (the
+//                           reference's friends layout, build_friends_list.cl:
+//                           1-21); a warp of consecutive particles reads one
+//                           row coalesced.
+//   meta                  : uint2[N] per particle: 7-bit friend count of each
+//                           of up to 8 circles (bits 0-55), the circles the
+//                           density pass keeps (bits 56-59) and the circles
+//                           the other passes keep (bits 60-63).
 
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -124,10 +128,13 @@ __global__ void reset_cells_kernel(int n, const uint32_t* __restrict__ keys, uin
 }
 
 // -------------------------------------------------------------- friends --
-// Packed per-circle counters: 8 circles x 8 bits (counts <= 64).
 __device__ __forceinline__ uint32_t byte_of(uint64_t v, int k) { return (uint32_t)(v >> (8 * k)) & 0xFFu; }
-__device__ __forceinline__ uint32_t half_of(uint64_t lo, uint64_t hi, int k) {
-    return (uint32_t)((k < 4 ? lo : hi) >> (16 * (k & 3))) & 0xFFFFu;
+__device__ __forceinline__ uint32_t circle_count(uint64_t meta, int k) { return (uint32_t)(meta >> (7 * k)) & 0x7Fu; }
+__device__ __forceinline__ int kept_density(uint64_t meta) { return (int)(meta >> 56) & 0xF; }
+__device__ __forceinline__ int kept_other(uint64_t meta) { return (int)(meta >> 60) & 0xF; }
+__device__ __forceinline__ uint64_t load_meta(const uint2* meta, int i) {
+    const uint2 m = meta[i];
+    return (uint64_t)m.x | ((uint64_t)m.y << 32);
 }
 
 // Number of leading circles a pass keeps: circles are visited in order and
@@ -144,13 +151,14 @@ __device__ __forceinline__ int circles_kept(uint64_t cnt, int C, int total, floa
     return kept;
 }
 
-// build_friends_list.cl:29-102.  Two scans of the 27 neighbour cells: the
-// first counts friends per circle (dropping those beyond particlesPerCircle,
-// :79-83), the second writes the ones the density pass will read in
-// circle-major order, which is the order every later pass sums in.
+// build_friends_list.cl:29-102: one scan of the 27 neighbour cells in the
+// reference's order (x, then y, then z offsets; particles of a cell in sorted
+// order), self excluded, r^2 < h^2, binned into circles by
+// min(int(adj^3 * C), C-1) with adj = max(0, (r - 0.3h) / 0.7h), at most
+// perCircle per circle (later ones are dropped, :79-83).
 __global__ void __launch_bounds__(kBlock)
 build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* __restrict__ cells,
-                     uint32_t* __restrict__ list, uint32_t* __restrict__ counts, int* __restrict__ err) {
+                     uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
     if (i >= n) return;
@@ -158,55 +166,55 @@ build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* 
     const int cx = __float2int_rz(pi.x / c.h), cy = __float2int_rz(pi.y / c.h), cz = __float2int_rz(pi.z / c.h);
     const int C = c.circles, P = c.perCircle;
     const float fC = (float)C;
-
-    uint64_t cnt = 0;
-    for (int pass = 0; pass < 2; ++pass) {
-        int keptL = 0;
-        uint64_t offLo = 0, offHi = 0, run = 0;
-        if (pass == 1) {
-            int total = 0;
-            for (int k = 0; k < C; ++k) total += (int)byte_of(cnt, k);
-            keptL = circles_kept(cnt, C, total, 0.6f);
-            const int keptD = circles_kept(cnt, C, total, 0.5f);
-            uint32_t acc = 0, nL = 0, nD = 0;
-            for (int k = 0; k < C; ++k) {
-                if (k < 4) offLo |= (uint64_t)acc << (16 * k); else offHi |= (uint64_t)acc << (16 * (k - 4));
-                acc += byte_of(cnt, k);
-                if (k < keptL) nL = acc;
-                if (k < keptD) nD = acc;
-            }
-            counts[i] = nL | (nD << 16);
-            if (keptL == 0) return;
-        }
-        for (int x = -1; x <= 1; ++x)
-            for (int y = -1; y <= 1; ++y)
-                for (int z = -1; z <= 1; ++z) {
-                    const uint2 range = cells[grid_hash(cx + x, cy + y, cz + z, c.grid)];
-                    if (range.x == kEmpty) continue;
-                    const uint32_t last = min(range.y, (uint32_t)(n - 1));
-                    if (range.x > last) { atomicOr(err, 1); continue; }
-                    for (uint32_t j = range.x; j <= last; ++j) {
-                        if ((int)j == i) continue;
-                        const float4 pj = pred[j];
-                        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-                        if (r2 >= c.h2) continue;
-                        const float adj = fmaxf(0.0f, (sqrtf(r2) - c.minR) / c.hMinusMinR);
-                        const int circ = min(__float2int_rz(adj * adj * adj * fC), C - 1);
-                        if (pass == 0) {
-                            if ((int)byte_of(cnt, circ) >= P) continue;
-                            cnt += 1ull << (8 * circ);
-                        } else {
-                            if (circ >= keptL) continue;
-                            const uint32_t r = byte_of(run, circ);
-                            if ((int)r >= P) continue;
-                            run += 1ull << (8 * circ);
-                            const uint32_t slot = half_of(offLo, offHi, circ) + r;
-                            list[(size_t)slot * n + i] = j;
-                        }
-                    }
+    uint64_t cnt = 0;  // 8 circles x 8-bit counters
+    for (int x = -1; x <= 1; ++x)
+        for (int y = -1; y <= 1; ++y)
+            for (int z = -1; z <= 1; ++z) {
+                const uint2 range = cells[grid_hash(cx + x, cy + y, cz + z, c.grid)];
+                if (range.x == kEmpty) continue;
+                const uint32_t last = min(range.y, (uint32_t)(n - 1));
+                if (range.x > last) { atomicOr(err, 1); continue; }
+                for (uint32_t j = range.x; j <= last; ++j) {
+                    if ((int)j == i) continue;
+                    const float4 pj = pred[j];
+                    const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                    const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+                    if (r2 >= c.h2) continue;
+                    const float adj = fmaxf(0.0f, (sqrtf(r2) - c.minR) / c.hMinusMinR);
+                    const int circ = min(__float2int_rz(adj * adj * adj * fC), C - 1);
+                    const uint32_t k = byte_of(cnt, circ);
+                    if ((int)k >= P) continue;
+                    list[(size_t)(circ * P + (int)k) * n + i] = j;
+                    cnt += 1ull << (8 * circ);
                 }
+            }
+    int total = 0;
+    uint64_t m = 0;
+    for (int k = 0; k < C; ++k) {
+        total += (int)byte_of(cnt, k);
+        m |= (uint64_t)byte_of(cnt, k) << (7 * k);
     }
+    m |= (uint64_t)circles_kept(cnt, C, total, 0.6f) << 56;
+    m |= (uint64_t)circles_kept(cnt, C, total, 0.5f) << 60;
+    meta[i] = make_uint2((uint32_t)m, (uint32_t)(m >> 32));
+}
+
+// Visit the friends of particle i that a pass keeps, circle by circle, each
+// circle in the order it was filled: the summation order of the reference.
+template <typename F>
+__device__ __forceinline__ void for_each_friend(const uint32_t* __restrict__ list, int n, int i, int perCircle,
+                                                uint64_t meta, int kept, F&& f) {
+    for (int k = 0; k < kept; ++k) {
+        const uint32_t m = circle_count(meta, k);
+        const uint32_t* row = list + (size_t)(k * perCircle) * n + i;
+        for (uint32_t s = 0; s < m; ++s) f(row[(size_t)s * n]);
+    }
+}
+
+// A neighbour enters the solver sums when r^2 < h^2 and, with the
+// zero-distance guard, r^2 > 0.
+__device__ __forceinline__ bool in_support(const DevConsts& c, float r2) {
+    return r2 < c.h2 && (!c.guard || r2 > 0.0f);
 }
 
 // -------------------------------------------------------------- scaling --
@@ -214,19 +222,18 @@ build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* 
 __global__ void __launch_bounds__(kBlock)
 compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __restrict__ predPacked,
                        float* __restrict__ density, const uint32_t* __restrict__ list,
-                       const uint32_t* __restrict__ counts) {
+                       const uint2* __restrict__ meta) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
     if (i >= n) return;
     const float4 pi = pred[i];
-    const uint32_t nl = counts[i] & 0xFFFFu;
+    const uint64_t mt = load_meta(meta, i);
     float ds = 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
-    for (uint32_t s = 0; s < nl; ++s) {
-        const uint32_t j = list[(size_t)s * n + i];
+    for_each_friend(list, n, i, c.perCircle, mt, kept_density(mt), [&](const uint32_t j) {
         const float4 pj = pred[j];
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-        if (r2 < c.h2) {
+        if (in_support(c, r2)) {
             const float rl = sqrtf(r2);
             const float hr = c.h - rl;
             const float sc = c.gradSpiky * hr * hr;
@@ -238,7 +245,7 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
             gy = gy + g1;
             gz = gz + g2;
         }
-    }
+    });
     ds = ds * c.poly6;
     density[i] = ds;
     gsk = gsk + dot3(gx, gy, gz, gx, gy, gz);
@@ -255,19 +262,18 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
 __global__ void __launch_bounds__(kBlock)
 compute_delta_kernel(DevConsts c, const float4* __restrict__ pp, float4* __restrict__ predOut,
                      const float* __restrict__ density, const uint32_t* __restrict__ list,
-                     const uint32_t* __restrict__ counts, int lastIteration) {
+                     const uint2* __restrict__ meta, int lastIteration) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
     if (i >= n) return;
     const float4 pi = pp[i];
-    const uint32_t nd = counts[i] >> 16;
+    const uint64_t mt = load_meta(meta, i);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    for (uint32_t s = 0; s < nd; ++s) {
-        const uint32_t j = list[(size_t)s * n + i];
+    for_each_friend(list, n, i, c.perCircle, mt, kept_other(mt), [&](const uint32_t j) {
         const float4 pj = pp[j];
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-        if (r2 < c.h2) {
+        if (in_support(c, r2)) {
             const float rl = sqrtf(r2);
             const float hr = c.h - rl;
             const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
@@ -280,7 +286,7 @@ compute_delta_kernel(DevConsts c, const float4* __restrict__ pp, float4* __restr
             sy = sy + a * g1;
             sz = sz + a * g2;
         }
-    }
+    });
     float fx = pi.x + (c.negGradSpiky * sx) / c.rho0;
     float fy = pi.y + (c.negGradSpiky * sy) / c.rho0;
     float fz = pi.z + (c.negGradSpiky * sz) / c.rho0;
@@ -314,19 +320,18 @@ __global__ void update_velocities_kernel(DevConsts c, const float4* __restrict__
 __global__ void __launch_bounds__(kBlock)
 apply_viscosity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ velIn,
                        float4* __restrict__ velOut, float4* __restrict__ omega,
-                       const uint32_t* __restrict__ list, const uint32_t* __restrict__ counts) {
+                       const uint32_t* __restrict__ list, const uint2* __restrict__ meta) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
     if (i >= n) return;
     const float4 pi = pred[i], vi = velIn[i];
-    const uint32_t nd = counts[i] >> 16;
+    const uint64_t mt = load_meta(meta, i);
     float vsx = 0.0f, vsy = 0.0f, vsz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
-    for (uint32_t s = 0; s < nd; ++s) {
-        const uint32_t j = list[(size_t)s * n + i];
+    for_each_friend(list, n, i, c.perCircle, mt, kept_other(mt), [&](const uint32_t j) {
         const float4 pj = pred[j];
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
-        if (r2 < c.h2 && fabsf(pj.w) > 1e-8f) {
+        if (in_support(c, r2) && fabsf(pj.w) > 1e-8f) {
             const float4 vj = velIn[j];
             const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
             const float d = c.h2 - r2;
@@ -341,7 +346,7 @@ apply_viscosity_kernel(DevConsts c, const float4* __restrict__ pred, const float
             vsy = vsy + uy * d3;
             vsz = vsz + uz * d3;
         }
-    }
+    });
     vsx = vsx * c.poly6;
     vsy = vsy * c.poly6;
     vsz = vsz * c.poly6;
@@ -353,19 +358,18 @@ apply_viscosity_kernel(DevConsts c, const float4* __restrict__ pred, const float
 __global__ void __launch_bounds__(kBlock)
 apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
                        const float4* __restrict__ velIn, float4* __restrict__ velOut,
-                       const uint32_t* __restrict__ list, const uint32_t* __restrict__ counts) {
+                       const uint32_t* __restrict__ list, const uint2* __restrict__ meta) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
     if (i >= n) return;
     const float4 pi = pred[i];
-    const uint32_t nd = counts[i] >> 16;
+    const uint64_t mt = load_meta(meta, i);
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    for (uint32_t s = 0; s < nd; ++s) {
-        const uint32_t j = list[(size_t)s * n + i];
+    for_each_friend(list, n, i, c.perCircle, mt, kept_other(mt), [&](const uint32_t j) {
         const float4 pj = pred[j];
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
-        if (r2 < c.h2 && fabsf(pj.w) > 1e-8f) {
+        if (in_support(c, r2) && fabsf(pj.w) > 1e-8f) {
             const float rl = sqrtf(r2);
             const float hr = c.h - rl;
             const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
@@ -375,7 +379,7 @@ apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float
             ey = ey + ol * g1;
             ez = ez + ol * g2;
         }
-    }
+    });
     ex = ex * c.negGradSpiky;
     ey = ey * c.negGradSpiky;
     ez = ez * c.negGradSpiky;
@@ -419,19 +423,19 @@ void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream
 }
 
 void launch_build_friends(const DevConsts& c, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint32_t* counts, int* errorWord, cudaStream_t s) {
+                          uint2* meta, int* errorWord, cudaStream_t s) {
     build_friends_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, reinterpret_cast<const uint2*>(cells), list,
-                                                            counts, errorWord);
+                                                            meta, errorWord);
 }
 
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
-                            const uint32_t* list, const uint32_t* counts, cudaStream_t s) {
-    compute_scaling_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, predPacked, density, list, counts);
+                            const uint32_t* list, const uint2* meta, cudaStream_t s) {
+    compute_scaling_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, predPacked, density, list, meta);
 }
 
 void launch_compute_delta(const DevConsts& c, const float4* predPacked, float4* predOut, const float* density,
-                          const uint32_t* list, const uint32_t* counts, int lastIteration, cudaStream_t s) {
-    compute_delta_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, predPacked, predOut, density, list, counts,
+                          const uint32_t* list, const uint2* meta, int lastIteration, cudaStream_t s) {
+    compute_delta_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, predPacked, predOut, density, list, meta,
                                                             lastIteration);
 }
 
@@ -441,13 +445,13 @@ void launch_update_velocities(const DevConsts& c, const float4* pred, const floa
 }
 
 void launch_apply_viscosity(const DevConsts& c, const float4* pred, const float4* velIn, float4* velOut,
-                            float4* omega, const uint32_t* list, const uint32_t* counts, cudaStream_t s) {
-    apply_viscosity_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, velIn, velOut, omega, list, counts);
+                            float4* omega, const uint32_t* list, const uint2* meta, cudaStream_t s) {
+    apply_viscosity_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, velIn, velOut, omega, list, meta);
 }
 
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
-                            float4* velOut, const uint32_t* list, const uint32_t* counts, cudaStream_t s) {
-    apply_vorticity_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, omega, velIn, velOut, list, counts);
+                            float4* velOut, const uint32_t* list, const uint2* meta, cudaStream_t s) {
+    apply_vorticity_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, omega, velIn, velOut, list, meta);
 }
 
 }  // namespace pbf

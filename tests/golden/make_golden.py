@@ -55,7 +55,8 @@ SEED = 20240601
 
 def scene(dims, overrides):
     params = pbf.load_scenario(overrides.get("base", "dam_break_32k"))
-    params.boxClamp = 0
+    params.boxClamp = 0            # stages the reference does not have
+    params.zeroDistanceGuard = 0
     for k, v in overrides.items():
         if k == "base":
             continue
@@ -90,7 +91,7 @@ def main() -> None:
         "generator": "tests/golden/make_golden.py",
         "source": "reference assets/kernels/*.cl compiled through oracle/clshim.hpp (oracle/_ref)",
         "scene": {"spacing": 0.05, "origin": [0.025, 0.025, 0.025], "jitter": 0.005, "seed": SEED,
-                  "base_par": "dam_break_32k", "boxClamp": 0},
+                  "base_par": "dam_break_32k", "boxClamp": 0, "zeroDistanceGuard": 0},
         "cases": [],
     }
     for name, dims, overrides, substeps in CASES:

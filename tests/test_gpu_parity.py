@@ -197,12 +197,13 @@ def test_rollout_300_frames_bit_exact(pbf_mod, oracle_mod, cuda_device):
             assert_same(f"vel@{cp}", gv, ov)
             assert_same(f"pred@{cp}", gpr, opr)
             rho = gpr[:, 3]
-            ok = np.isfinite(rho)
+            ok = np.isfinite(gp).all(axis=1) & np.isfinite(gv).all(axis=1) & np.isfinite(rho)
             err = np.abs(rho[ok] / params.restDensity - 1.0)
             ke = 0.5 * np.sum(gv[ok, :3].astype(np.float64) ** 2)
             pe = params.garvity * np.sum(gp[ok, 1].astype(np.float64))
             print(f"substep {cp}: density error mean {err.mean():.4f} max {err.max():.3f}; "
                   f"kinetic {ke:.2f} potential {pe:.2f}; non-finite {int((~ok).sum())}")
+            assert ok.all(), "the guarded scene keeps every particle finite"
 
 
 def test_one_substep_at_1m_bit_exact_and_fp64_error(pbf_mod, oracle_mod, cuda_device):
