@@ -1,0 +1,151 @@
+// pbf_simulation.hpp — C++ facade with the reference's host interface.
+//
+// Mirrors src/Simulation.hpp:28-151 and src/ParamUtils.hpp: a global
+// `Parameters Params`, `LoadParameters(std::string)`, and a class
+// `Simulation` whose InitBuffers / InitCells / LoadForceMasks / InitKernels /
+// Step keep their names, order and meaning.  Differences a caller sees:
+//   - the constructor takes a CUDA device ordinal instead of an OpenCL
+//     context and device (Simulation.cpp:56-63);
+//   - positions live in device memory owned by the library, not in GL
+//     buffers: DevicePositions() gives their address, ReadState() copies them
+//     out (the reference's mSharedPingBufferID / mSharedPongBufferID);
+//   - errors are thrown as std::runtime_error carrying the library's message
+//     (the reference throws cl::Error / std::runtime_error), and InitKernels
+//     returns false on a parameter set the kernels cannot run, as the
+//     reference returns false on a build failure (Simulation.cpp:186-188).
+// Header-only over include/pbf_capi.h; link with libpbf_gb300.so.
+#pragma once
+
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "pbf_capi.h"
+
+typedef PbfParameters Parameters;
+
+// src/ParamUtils.cpp:19-22: the global parameter set, zero-initialised.
+inline Parameters Params = {};
+inline bool ParametersChanged = false;
+
+// src/ParamUtils.cpp:24-100
+inline void LoadParameters(std::string fileContents) {
+    if (pbf_load_parameters(fileContents.c_str(), &Params, nullptr) != PBF_OK)
+        throw std::runtime_error(pbf_last_error(nullptr));
+    ParametersChanged = true;
+}
+
+// Per-stage device times, in the reference tracker names (src/OCLPerfMon.h).
+struct PerfTracker {
+    std::string eventName;
+    double total_time;  // milliseconds, exponentially smoothed with weight 0.5
+};
+
+class Simulation {
+public:
+    explicit Simulation(int device = 0) : mDevice(device) {}
+    ~Simulation() { pbf_destroy(mCtx); }
+    Simulation(const Simulation&) = delete;
+    Simulation& operator=(const Simulation&) = delete;
+
+    // Simulation::InitBuffers (src/Simulation.cpp:206-244): buffers for
+    // Params.particleCount particles, initial positions from `pos` (float4 per
+    // particle) or the reference's CreateParticles lattice, velocities from
+    // `vel` or zero.
+    void InitBuffers(const float* pos = nullptr, const float* vel = nullptr) {
+        pbf_destroy(mCtx);
+        mCtx = nullptr;
+        check(pbf_create(&Params, mDevice, &mCtx), nullptr);
+        check(pbf_init_buffers(mCtx, pos, vel));
+    }
+
+    // Simulation::InitCells (src/Simulation.cpp:246-255)
+    void InitCells() {
+        syncParams(false);
+        check(pbf_init_cells(mCtx));
+    }
+
+    // Simulation::LoadForceMasks (src/Simulation.cpp:257-281): the empty mask.
+    void LoadForceMasks() { check(pbf_load_force_masks(mCtx, nullptr, 0, 0)); }
+
+    // Simulation::InitKernels (src/Simulation.cpp:129-204)
+    bool InitKernels() {
+        if (!mCtx) return false;
+        if (pbf_set_params(mCtx, &Params) != PBF_OK) return false;
+        return pbf_init_kernels(mCtx) == PBF_OK;
+    }
+
+    // Simulation::Step (src/Simulation.cpp:554-621): one substep, synchronous.
+    void Step() {
+        check(pbf_set_pause(mCtx, bPauseSim ? 1 : 0));
+        if (mTrack) check(pbf_enable_stage_timing(mCtx, 1));
+        check(pbf_step(mCtx, 1));
+        if (mTrack) updateTimings();
+    }
+
+    // Simulation::KernelFileList (src/Simulation.cpp:103-127): the sources
+    // the device code is built from.
+    const std::string* KernelFileList() {
+        static const std::string files[] = {"pbf_kernels.cu", "pbf_sort.cu", "pbf_capi.cu", ""};
+        return files;
+    }
+
+    // ---- state access replacing the GL-shared buffers ----
+    void* DevicePositions() {
+        void* p = nullptr;
+        check(pbf_device_positions(mCtx, &p));
+        return p;
+    }
+    void ReadState(float* pos, float* vel, float* pred = nullptr) { check(pbf_read_state(mCtx, pos, vel, pred)); }
+    void WriteState(const float* pos, const float* vel) { check(pbf_write_state(mCtx, pos, vel)); }
+
+    // Turns the per-stage trackers on (each Step then times its stages).
+    void TrackPerformance(bool on) {
+        mTrack = on;
+        check(pbf_enable_stage_timing(mCtx, on ? 1 : 0));
+    }
+
+    pbf_ctx* handle() const { return mCtx; }
+
+    bool bPauseSim = false;
+    std::vector<PerfTracker> PerfData;
+
+private:
+    void check(int rc, pbf_ctx* ctx) const {
+        if (rc != PBF_OK) throw std::runtime_error(pbf_last_error(ctx));
+    }
+    void check(int rc) const { check(rc, mCtx); }
+
+    void syncParams(bool strict) {
+        if (!mCtx) throw std::runtime_error("InitBuffers must run first");
+        int rc = pbf_set_params(mCtx, &Params);
+        if (strict) check(rc);
+    }
+
+    // OCLPerfMon::UpdateTimings (src/OCLPerfMon.cpp:36-51): EMA with weight 0.5.
+    void updateTimings() {
+        float ms[64];
+        int count = 0;
+        char names[2048];
+        check(pbf_stage_timings(mCtx, ms, 64, &count, names, sizeof names));
+        std::vector<std::string> keys;
+        std::string all(names), cur;
+        for (char ch : all) {
+            if (ch == '\n') { keys.push_back(cur); cur.clear(); }
+            else cur += ch;
+        }
+        if (!cur.empty()) keys.push_back(cur);
+        for (int k = 0; k < count && k < (int)keys.size(); ++k) {
+            PerfTracker* t = nullptr;
+            for (auto& e : PerfData)
+                if (e.eventName == keys[k]) t = &e;
+            if (!t) { PerfData.push_back({keys[k], 0.0}); t = &PerfData.back(); }
+            t->total_time = ms[k] * 0.5 + t->total_time * 0.5;
+        }
+    }
+
+    int mDevice = 0;
+    pbf_ctx* mCtx = nullptr;
+    bool mTrack = false;
+};
