@@ -180,6 +180,39 @@ int pbf_launch_count(pbf_ctx* ctx, uint64_t* count);
 /* Use (1) or stop using (0) a captured CUDA graph for each substep. */
 int pbf_use_graph(pbf_ctx* ctx, int enable);
 
+/* ------------------------------------------------ allocation-free variant -- */
+
+/* Largest particle count pbf_sort_state_noalloc accepts, and the size of the
+   fixed working array it keeps on every GPU that loads this library (held
+   until the process exits). */
+#define PBF_NOALLOC_MAX_KEYS       (1u << 20)
+#define PBF_NOALLOC_SCRATCH_BYTES  8650752u   /* 8.25 MiB */
+
+/* The key / sort / cell-table stage of pbf_sort_state for callers that may
+   not allocate device memory: hosts that reserve all device memory at start-up
+   and forbid allocations afterwards (real-time frame loops, engines that own
+   the GPU's memory budget).  It has no counterpart in the reference.
+
+   Every pointer is a device address on the calling thread's current device:
+     d_pred  : float4 x params->particleCount predicted positions (input),
+     d_keys  : params->particleCount sorted keys (output, no padding entries),
+     d_perm  : params->particleCount sort permutation (output),
+     d_cells : 2 * params->gridBufSize words of cell table (output; may be NULL).
+   The outputs equal the first particleCount keys / permutation entries and
+   the cell table of pbf_sort_state.  Work is enqueued on `stream` (a
+   cudaStream_t; NULL is the legacy default stream) and is complete when the
+   stream reaches it.
+
+   The call allocates nothing: its working memory is one fixed array of
+   PBF_NOALLOC_SCRATCH_BYTES per device, shared by every call on that device.
+   The first call on a device looks up that array's address (a runtime call,
+   no allocation); make that first call before any stream capture.  Calls
+   whose work overlaps on the GPU (e.g. on two streams at once) race on the
+   shared array and must be ordered by the caller.  particleCount above
+   PBF_NOALLOC_MAX_KEYS returns PBF_ERR_INVALID without enqueuing work. */
+int pbf_sort_state_noalloc(const PbfParameters* params, const float* d_pred,
+                           uint32_t* d_keys, uint32_t* d_perm, uint32_t* d_cells, void* stream);
+
 /* ------------------------------------------------------------- scenarios -- */
 
 /* The reference's initial lattice (Simulation::CreateParticles,

@@ -34,6 +34,7 @@ CUDA_UNITS = {
     "pbf_kernels.cu": ["--fmad=false"],
     "pbf_sort.cu": [],
     "pbf_capi.cu": ["--fmad=false"],
+    "pbf_noalloc.cu": ["--fmad=false"],
 }
 CXX_UNITS = ["params.cpp"]
 

@@ -104,6 +104,7 @@ def library() -> ctypes.CDLL:
         "pbf_use_graph": [c_void_p, c_int],
         "pbf_reference_lattice": [P, f32p],
         "pbf_scene_block": [c_int, c_int, c_int, c_float, c_float, c_float, c_float, c_float, c_uint64, f32p],
+        "pbf_sort_state_noalloc": [P, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -156,6 +157,12 @@ def scene_block(nx: int, ny: int, nz: int, spacing: float, origin=(0.0, 0.0, 0.0
     _check(library().pbf_scene_block(nx, ny, nz, spacing, float(origin[0]), float(origin[1]), float(origin[2]),
                                      jitter, seed, _f32(out)))
     return out
+
+
+def sort_state_noalloc(params: PbfParameters, d_pred: int, d_keys: int, d_perm: int, d_cells: int | None = None,
+                       stream: int | None = None) -> None:
+    """pbf_sort_state_noalloc on device addresses (see include/pbf_capi.h)."""
+    _check(library().pbf_sort_state_noalloc(ctypes.byref(params), d_pred, d_keys, d_perm, d_cells, stream))
 
 
 def reference_lattice(params: PbfParameters) -> np.ndarray:
@@ -331,7 +338,7 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_step", "pbf_step_async", "pbf_synchronize", "pbf_read_state", "pbf_write_state",
         "pbf_device_positions", "pbf_get_stream", "pbf_sort_state", "pbf_read_friends",
         "pbf_enable_stage_timing", "pbf_stage_timings", "pbf_launch_count", "pbf_use_graph",
-        "pbf_reference_lattice", "pbf_scene_block",
+        "pbf_reference_lattice", "pbf_scene_block", "pbf_sort_state_noalloc",
     ])
 
 
