@@ -199,17 +199,53 @@ build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* 
     meta[i] = make_uint2((uint32_t)m, (uint32_t)(m >> 32));
 }
 
-// Visit the friends of particle i that a pass keeps, circle by circle, each
-// circle in the order it was filled: the summation order of the reference.
-template <typename F>
-__device__ __forceinline__ void for_each_friend(const uint32_t* __restrict__ list, int n, int i, int perCircle,
-                                                uint64_t meta, int kept, F&& f) {
-    for (int k = 0; k < kept; ++k) {
-        const uint32_t m = circle_count(meta, k);
-        const uint32_t* row = list + (size_t)(k * perCircle) * n + i;
-        for (uint32_t s = 0; s < m; ++s) f(row[(size_t)s * n]);
+// The friends of particle i that a pass keeps, as one flat sequence
+// t = 0 .. total-1 in circle-major order (the reference's summation order):
+// entry t of circle k sits in list row t + (k*perCircle - first(k)), where
+// first(k) is the number of entries of the circles before k.
+struct FriendRows {
+    uint64_t meta;
+    int perCircle, total, k, boundary, off;
+    __device__ __forceinline__ FriendRows(uint64_t m, int kept, int P) : meta(m), perCircle(P), k(0), off(0) {
+        total = 0;
+        for (int c = 0; c < kept; ++c) total += (int)circle_count(m, c);
+        boundary = (int)circle_count(m, 0);
     }
+    // Rows are requested for t = 0, 1, 2, ... in order.
+    __device__ __forceinline__ int row(int t) {
+        while (t >= boundary) {
+            off += perCircle - (int)circle_count(meta, k);
+            ++k;
+            boundary += (int)circle_count(meta, k);
+        }
+        return t + off;
+    }
+};
+
+// Runs body(load(j)) for every kept friend j in order.  Neighbours are taken
+// U at a time: the U list entries are loaded, then the U neighbour records,
+// then the U bodies run in order, so the sums keep their sequential order
+// while U independent loads are in flight.
+template <int U, typename LoadF, typename BodyF>
+__device__ __forceinline__ void gather_friends(const uint32_t* __restrict__ list, int n, int i, FriendRows fr,
+                                               LoadF load, BodyF body) {
+    int t = 0;
+    for (; t + U <= fr.total; t += U) {
+        uint32_t j[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) j[u] = __ldg(list + (size_t)fr.row(t + u) * n + i);
+        decltype(load(0u)) rec[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) rec[u] = load(j[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) body(rec[u]);
+    }
+    for (; t < fr.total; ++t) body(load(__ldg(list + (size_t)fr.row(t) * n + i)));
 }
+
+struct PairRec {
+    float4 a, b;
+};
 
 // A neighbour enters the solver sums when r^2 < h^2 and, with the
 // zero-distance guard, r^2 > 0.
@@ -229,8 +265,9 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
     const float4 pi = pred[i];
     const uint64_t mt = load_meta(meta, i);
     float ds = 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
-    for_each_friend(list, n, i, c.perCircle, mt, kept_density(mt), [&](const uint32_t j) {
-        const float4 pj = pred[j];
+    constexpr int U = 4;
+    gather_friends<U>(list, n, i, FriendRows(mt, kept_density(mt), c.perCircle),
+                      [&](uint32_t j) { return __ldg(pred + j); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = dot3(rx, ry, rz, rx, ry, rz);
         if (in_support(c, r2)) {
@@ -269,8 +306,9 @@ compute_delta_kernel(DevConsts c, const float4* __restrict__ pp, float4* __restr
     const float4 pi = pp[i];
     const uint64_t mt = load_meta(meta, i);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    for_each_friend(list, n, i, c.perCircle, mt, kept_other(mt), [&](const uint32_t j) {
-        const float4 pj = pp[j];
+    constexpr int U = 4;
+    gather_friends<U>(list, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
+                      [&](uint32_t j) { return __ldg(pp + j); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = dot3(rx, ry, rz, rx, ry, rz);
         if (in_support(c, r2)) {
@@ -327,12 +365,14 @@ apply_viscosity_kernel(DevConsts c, const float4* __restrict__ pred, const float
     const float4 pi = pred[i], vi = velIn[i];
     const uint64_t mt = load_meta(meta, i);
     float vsx = 0.0f, vsy = 0.0f, vsz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
-    for_each_friend(list, n, i, c.perCircle, mt, kept_other(mt), [&](const uint32_t j) {
-        const float4 pj = pred[j];
+    constexpr int U = 4;
+    gather_friends<U>(list, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
+                      [&](uint32_t j) { return PairRec{__ldg(pred + j), __ldg(velIn + j)}; }, [&](const PairRec& q) {
+        const float4 pj = q.a;
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
         if (in_support(c, r2) && fabsf(pj.w) > 1e-8f) {
-            const float4 vj = velIn[j];
+            const float4 vj = q.b;
             const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
             const float d = c.h2 - r2;
             const float rl = sqrtf(r2);
@@ -365,15 +405,17 @@ apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float
     const float4 pi = pred[i];
     const uint64_t mt = load_meta(meta, i);
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    for_each_friend(list, n, i, c.perCircle, mt, kept_other(mt), [&](const uint32_t j) {
-        const float4 pj = pred[j];
+    constexpr int U = 4;
+    gather_friends<U>(list, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
+                      [&](uint32_t j) { return PairRec{__ldg(pred + j), __ldg(omega + j)}; }, [&](const PairRec& q) {
+        const float4 pj = q.a;
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
         if (in_support(c, r2) && fabsf(pj.w) > 1e-8f) {
             const float rl = sqrtf(r2);
             const float hr = c.h - rl;
             const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
-            const float4 oj = omega[j];
+            const float4 oj = q.b;
             const float ol = sqrtf(dot3(oj.x, oj.y, oj.z, oj.x, oj.y, oj.z));
             ex = ex + ol * g0;
             ey = ey + ol * g1;

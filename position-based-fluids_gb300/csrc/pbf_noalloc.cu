@@ -27,7 +27,7 @@ namespace {
 
 constexpr size_t kMaxKeys = PBF_NOALLOC_MAX_KEYS;
 constexpr size_t kTileKeys = 4096;                            // keys per radix-sort tile (pbf_sort.cu)
-constexpr size_t kHistWords = 256 * (kMaxKeys / kTileKeys);   // one 256-bin histogram per tile
+constexpr size_t kHistWords = 256 * (kMaxKeys / kTileKeys) + 256;  // a 256-bin histogram per tile + digit totals
 constexpr size_t kScratchWords = 2 * kMaxKeys + kHistWords;   // keys + permutation ping-pong, histograms
 static_assert(kScratchWords * 4 == PBF_NOALLOC_SCRATCH_BYTES, "scratch size stated in pbf_capi.h");
 

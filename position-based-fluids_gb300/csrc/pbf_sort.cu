@@ -8,7 +8,9 @@
 // Here the keys are < gridBufSize, so only ceil(log2(gridBufSize) / 8)
 // passes of 8-bit digits are run (3 at gridBufSize = 2^19).  Each pass is
 //   upsweep   : per-tile 256-bin digit histogram -> hist[digit][tile]
-//   scan      : one exclusive scan over hist in [digit][tile] order
+//   scan      : per digit, an exclusive scan over the tiles (one block per
+//               digit); the downsweep adds the exclusive scan of the digit
+//               totals
 //   downsweep : per-warp stable ranking with __match_any_sync and per-warp
 //               digit counters in shared memory, then the scatter.
 // A tile is 4096 keys: 8 warps, each owning 512 consecutive keys taken in 16
@@ -27,7 +29,6 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kRounds = 16;
 constexpr int kTile = kThreads * kRounds;   // 4096 keys
 constexpr int kWarpKeys = 32 * kRounds;     // 512 keys
-constexpr int kScanThreads = 1024;
 
 __global__ void __launch_bounds__(kThreads)
 radix_upsweep_kernel(const uint32_t* __restrict__ keys, int n, int shift, int tiles, uint32_t* __restrict__ hist) {
@@ -44,53 +45,64 @@ radix_upsweep_kernel(const uint32_t* __restrict__ keys, int n, int shift, int ti
     hist[(size_t)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of `total` words in place by one block: each thread sums a
-// contiguous chunk, the chunk sums are scanned across the block, and the
-// chunks are rewritten.
-__global__ void __launch_bounds__(kScanThreads)
-radix_scan_kernel(uint32_t* __restrict__ hist, int total) {
-    __shared__ uint32_t warpSums[kScanThreads / 32];
+// Per-digit exclusive scan over the tiles: block d scans row d of
+// hist[digit][tile] in place and writes the row's total to totals[d].
+__global__ void __launch_bounds__(kThreads)
+radix_scan_kernel(uint32_t* __restrict__ hist, int tiles, uint32_t* __restrict__ totals) {
+    __shared__ uint32_t warpSums[kWarps];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const int chunk = (total + kScanThreads - 1) / kScanThreads;
-    const int begin = min(t * chunk, total), end = min(begin + chunk, total);
-    uint32_t sum = 0;
-    for (int k = begin; k < end; ++k) sum += hist[k];
-    // inclusive warp scan of the chunk sums
-    uint32_t incl = sum;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-        if (lane >= d) incl += v;
-    }
-    if (lane == 31) warpSums[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = warpSums[lane];
+    uint32_t* row = hist + (size_t)blockIdx.x * tiles;
+    uint32_t carry = 0;
+    for (int base = 0; base < tiles; base += kThreads) {
+        const int k = base + t;
+        const uint32_t v = k < tiles ? row[k] : 0u;
+        uint32_t incl = v;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, w, d);
-            if (lane >= d) w += v;
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= d) incl += u;
         }
-        warpSums[lane] = w;
+        if (lane == 31) warpSums[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0, all = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t ws = warpSums[w];
+            before += w < warp ? ws : 0u;
+            all += ws;
+        }
+        if (k < tiles) row[k] = carry + before + incl - v;
+        carry += all;
+        __syncthreads();
     }
-    __syncthreads();
-    uint32_t run = incl - sum + (warp > 0 ? warpSums[warp - 1] : 0u);
-    for (int k = begin; k < end; ++k) {
-        const uint32_t v = hist[k];
-        hist[k] = run;
-        run += v;
-    }
+    if (t == 0) totals[blockIdx.x] = carry;
 }
 
 __global__ void __launch_bounds__(kThreads)
 radix_downsweep_kernel(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ permIn,
                        uint32_t* __restrict__ keysOut, uint32_t* __restrict__ permOut, int n, int shift,
-                       int tiles, const uint32_t* __restrict__ hist) {
+                       int tiles, const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals) {
     __shared__ uint32_t warpCount[kWarps][256];
     __shared__ uint32_t digitBase[256];
+    __shared__ uint32_t warpSums[kWarps];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
 #pragma unroll
     for (int w = 0; w < kWarps; ++w) warpCount[w][t] = 0;
+    {   // digitBase[d] = keys of all tiles with a smaller digit (exclusive scan of the totals)
+        const uint32_t v = totals[t];
+        uint32_t incl = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= d) incl += u;
+        }
+        if (lane == 31) warpSums[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) before += w < warp ? warpSums[w] : 0u;
+        digitBase[t] = before + incl - v;
+    }
     __syncthreads();
 
     const size_t base = (size_t)blockIdx.x * kTile + (size_t)warp * kWarpKeys;
@@ -124,7 +136,7 @@ radix_downsweep_kernel(const uint32_t* __restrict__ keysIn, const uint32_t* __re
             warpCount[w][t] = run;
             run += c;
         }
-        digitBase[t] = hist[(size_t)t * tiles + blockIdx.x];
+        digitBase[t] += hist[(size_t)t * tiles + blockIdx.x];
     }
     __syncthreads();
 #pragma unroll
@@ -148,7 +160,7 @@ SortPlan make_sort_plan(int n, uint32_t gridBufSize) {
     while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)gridBufSize) ++bits;  // keys <= gridBufSize-1
     p.passes = (bits + 7) / 8;
     p.tiles = (n + kTile - 1) / kTile;
-    p.histWords = (size_t)256 * p.tiles;
+    p.histWords = (size_t)256 * p.tiles + 256;  // per-tile histograms, then the 256 digit totals
     return p;
 }
 
@@ -157,12 +169,13 @@ int radix_sort_launches(const SortPlan& plan) { return 3 * plan.passes; }
 int launch_radix_sort(const SortPlan& plan, uint32_t* keys[2], uint32_t* perm[2], uint32_t* hist,
                       const float4*, const float4*, float4*, float4*, cudaStream_t s) {
     int cur = 0;
+    uint32_t* totals = hist + (size_t)256 * plan.tiles;
     for (int pass = 0; pass < plan.passes; ++pass) {
         const int shift = 8 * pass;
         radix_upsweep_kernel<<<plan.tiles, kThreads, 0, s>>>(keys[cur], plan.n, shift, plan.tiles, hist);
-        radix_scan_kernel<<<1, kScanThreads, 0, s>>>(hist, (int)plan.histWords);
+        radix_scan_kernel<<<256, kThreads, 0, s>>>(hist, plan.tiles, totals);
         radix_downsweep_kernel<<<plan.tiles, kThreads, 0, s>>>(keys[cur], perm[cur], keys[cur ^ 1], perm[cur ^ 1],
-                                                               plan.n, shift, plan.tiles, hist);
+                                                               plan.n, shift, plan.tiles, hist, totals);
         cur ^= 1;
     }
     return cur;
