@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -89,6 +90,41 @@ static float six_digit_literal(double v) {
     return std::strtof(buf, nullptr);
 }
 
+// Friend circle of a neighbour at squared distance r2 (< h^2), evaluated as
+// build_friends_list.cl:75-76 does, one IEEE operation at a time.
+static int circle_of(float r2, float minR, float hMinusMinR, int C) {
+    const float adj = std::fmax(0.0f, (std::sqrt(r2) - minR) / hMinusMinR);
+    const int circ = (int)(adj * adj * adj * (float)C);
+    return circ < C - 1 ? circ : C - 1;
+}
+
+// Every operation in circle_of rounds monotonically, so the circle is a
+// non-decreasing step function of r2 (r2 >= 0).  For each k, bisect over the
+// bit patterns of the non-negative floats below h^2 for the first r2 whose
+// circle reaches k.
+static void circle_thresholds(DevConsts& c) {
+    for (int k = 0; k < PBF_MAX_CIRCLES; ++k) c.circT[k] = INFINITY;
+    uint32_t h2bits;
+    std::memcpy(&h2bits, &c.h2, 4);
+    for (int k = 1; k < c.circles; ++k) {
+        auto circ = [&](uint32_t bits) {
+            float r2;
+            std::memcpy(&r2, &bits, 4);
+            return circle_of(r2, c.minR, c.hMinusMinR, c.circles);
+        };
+        if (h2bits == 0 || circ(h2bits - 1) < k) continue;  // no r2 < h^2 reaches k
+        if (circ(0) >= k) { c.circT[k - 1] = 0.0f; continue; }
+        uint32_t lo = 0, hi = h2bits - 1;  // circ(lo) < k <= circ(hi)
+        while (hi - lo > 1) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (circ(mid) >= k) hi = mid; else lo = mid;
+        }
+        float t;
+        std::memcpy(&t, &hi, 4);
+        c.circT[k - 1] = t;
+    }
+}
+
 DevConsts make_consts(const PbfParameters& p, int n) {
     DevConsts c{};
     const double kPi = 3.14159265358979323846;
@@ -120,6 +156,7 @@ DevConsts make_consts(const PbfParameters& p, int n) {
     c.perCircle = (int)p.particlesPerCircle;
     c.grid = p.gridBufSize;
     c.n = n;
+    if (c.circles >= 1 && c.circles <= PBF_MAX_CIRCLES && c.h2 > 0.0f) circle_thresholds(c);
     return c;
 }
 

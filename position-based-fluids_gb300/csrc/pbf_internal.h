@@ -23,6 +23,10 @@ struct DevConsts {
     int circles, perCircle;
     uint32_t grid;
     int n;
+    // circT[k-1]: the smallest r^2 whose friend circle is >= k (k = 1..C-1),
+    // +inf where no r^2 < h^2 reaches circle k.  The circle of r^2 is the
+    // number of thresholds it reaches.
+    float circT[PBF_MAX_CIRCLES];
 };
 
 // Records `msg` as the last error of `ctx` (or of the calling thread when ctx

@@ -155,7 +155,10 @@ __device__ __forceinline__ int circles_kept(uint64_t cnt, int C, int total, floa
 // reference's order (x, then y, then z offsets; particles of a cell in sorted
 // order), self excluded, r^2 < h^2, binned into circles by
 // min(int(adj^3 * C), C-1) with adj = max(0, (r - 0.3h) / 0.7h), at most
-// perCircle per circle (later ones are dropped, :79-83).
+// perCircle per circle (later ones are dropped, :79-83).  The 27 hashes are
+// formed from the three spread coordinates of each axis, and the circle is
+// read off precomputed r^2 thresholds (DevConsts::circT): the same integer
+// the sqrt / divide / cube / truncate sequence gives, without computing it.
 __global__ void __launch_bounds__(kBlock)
 build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* __restrict__ cells,
                      uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
@@ -165,38 +168,48 @@ build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* 
     const float4 pi = pred[i];
     const int cx = __float2int_rz(pi.x / c.h), cy = __float2int_rz(pi.y / c.h), cz = __float2int_rz(pi.z / c.h);
     const int C = c.circles, P = c.perCircle;
-    const float fC = (float)C;
+    const bool pow2 = (c.grid & (c.grid - 1)) == 0;
+    const uint32_t mask = c.grid - 1;
+    const uint32_t exm = expand_bits(cx - 1), ex0 = expand_bits(cx), exp_ = expand_bits(cx + 1);
+    const uint32_t eym = expand_bits(cy - 1) << 1, ey0 = expand_bits(cy) << 1, eyp = expand_bits(cy + 1) << 1;
+    const uint32_t ezm = expand_bits(cz - 1) << 2, ez0 = expand_bits(cz) << 2, ezp = expand_bits(cz + 1) << 2;
     uint64_t cnt = 0;  // 8 circles x 8-bit counters
-    for (int x = -1; x <= 1; ++x)
-        for (int y = -1; y <= 1; ++y)
+    for (int x = -1; x <= 1; ++x) {
+        const uint32_t ex = x < 0 ? exm : (x > 0 ? exp_ : ex0);
+        for (int y = -1; y <= 1; ++y) {
+            const uint32_t exy = ex | (y < 0 ? eym : (y > 0 ? eyp : ey0));
             for (int z = -1; z <= 1; ++z) {
-                const uint2 range = cells[grid_hash(cx + x, cy + y, cz + z, c.grid)];
+                const uint32_t m = exy | (z < 0 ? ezm : (z > 0 ? ezp : ez0));
+                const uint2 range = cells[pow2 ? (m & mask) : (m % c.grid)];
                 if (range.x == kEmpty) continue;
                 const uint32_t last = min(range.y, (uint32_t)(n - 1));
                 if (range.x > last) { atomicOr(err, 1); continue; }
                 for (uint32_t j = range.x; j <= last; ++j) {
                     if ((int)j == i) continue;
-                    const float4 pj = pred[j];
+                    const float4 pj = __ldg(pred + j);
                     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
                     const float r2 = dot3(rx, ry, rz, rx, ry, rz);
                     if (r2 >= c.h2) continue;
-                    const float adj = fmaxf(0.0f, (sqrtf(r2) - c.minR) / c.hMinusMinR);
-                    const int circ = min(__float2int_rz(adj * adj * adj * fC), C - 1);
+                    // thresholds past C-1 are +inf, so only the first C-1 decide
+                    int circ = (r2 >= c.circT[0]) + (r2 >= c.circT[1]) + (r2 >= c.circT[2]) + (r2 >= c.circT[3]);
+                    if (C > 5) circ += (r2 >= c.circT[4]) + (r2 >= c.circT[5]) + (r2 >= c.circT[6]);
                     const uint32_t k = byte_of(cnt, circ);
                     if ((int)k >= P) continue;
                     list[(size_t)(circ * P + (int)k) * n + i] = j;
                     cnt += 1ull << (8 * circ);
                 }
             }
+        }
+    }
     int total = 0;
-    uint64_t m = 0;
+    uint64_t mt = 0;
     for (int k = 0; k < C; ++k) {
         total += (int)byte_of(cnt, k);
-        m |= (uint64_t)byte_of(cnt, k) << (7 * k);
+        mt |= (uint64_t)byte_of(cnt, k) << (7 * k);
     }
-    m |= (uint64_t)circles_kept(cnt, C, total, 0.6f) << 56;
-    m |= (uint64_t)circles_kept(cnt, C, total, 0.5f) << 60;
-    meta[i] = make_uint2((uint32_t)m, (uint32_t)(m >> 32));
+    mt |= (uint64_t)circles_kept(cnt, C, total, 0.6f) << 56;
+    mt |= (uint64_t)circles_kept(cnt, C, total, 0.5f) << 60;
+    meta[i] = make_uint2((uint32_t)mt, (uint32_t)(mt >> 32));
 }
 
 // The friends of particle i that a pass keeps, as one flat sequence
