@@ -62,6 +62,14 @@ STAGE_BYTES = {
     "applyVorticity": lambda nl, nd: 68.0 + 4.0 * nd,
 }
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
+# density pass, from `ncu --set full` on this workload at an early frame where
+# the density pass used 22.3 friends per particle (profiles/
+# compute_scaling_dam_break_1m.md).  Its traffic is dominated by the
+# friend-list rows, so it is scaled to the timed state by the per-particle
+# algorithmic bytes (40 + 4 nl).
+TRAFFIC_CAPTURE = {"kernel": "computeScaling", "bytes": 165.92e6, "nl": 22.3}
+
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -267,6 +275,10 @@ def gpu_arm(args) -> None:
     algo_bytes = STAGE_BYTES[dominant](nl, nd) * n
     peak, peak_kind = measured_peaks()
     achieved = algo_bytes / (launch_ms / 1000.0) / 1e9
+    traffic = None
+    if dominant == TRAFFIC_CAPTURE["kernel"]:
+        scale = STAGE_BYTES[dominant](nl, nd) / STAGE_BYTES[dominant](TRAFFIC_CAPTURE["nl"], TRAFFIC_CAPTURE["nl"])
+        traffic = TRAFFIC_CAPTURE["bytes"] * scale
     frame_ms = ms / args.steps
     bytes_sub = (444.0 + 56.0 * iters) * n  # whole-substep compulsory bytes, P = 3 sort passes
     pipeline_gbs = bytes_sub * sub / (frame_ms / 1000.0) / 1e9
@@ -293,7 +305,7 @@ def gpu_arm(args) -> None:
                 "steps": e2e_steps},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": launch_ms},
         "pipeline_roofline": {"bytes_per_particle_substep": 444.0 + 56.0 * iters, "achieved": pipeline_gbs,
                               "frac": pipeline_gbs / peak},
