@@ -321,6 +321,67 @@ def gpu_arm(args) -> None:
         dist.destroy_process_group()
 
 
+# Stage groups of the particle-count sweep.
+SWEEP_GROUPS = {
+    "sort": ["predictPositions", "radixsort", "sortParticles", "updateCells", "resetPartList"],
+    "gather": ["buildFriendsList"],
+    "constraint": ["computeScaling", "computeDelta"],
+    "velocity": ["updateVelocities", "applyViscosity", "applyVorticity"],
+}
+
+
+def sweep(args) -> None:
+    """Particle-count sweep on the double dam break: one JSON line per
+    (particles, iterations) with stage-group times against HBM peak."""
+    import torch
+    import pbf
+    peak, peak_kind = measured_peaks()
+    counts = [int(x) for x in args.sweep_counts.split(",")]
+    for n in counts:
+        for iters in (2, 4, 8):
+            params, pos, vel = pbf.make_double_dam_break(n, iterations=iters)
+            sub = int(params.subSteps)
+            sim = pbf.Simulation.create(params, pos, vel, device=0)
+            stream = torch.cuda.ExternalStream(sim.stream())
+            for _ in range(args.sweep_warmup):
+                sim.step_async(sub)
+            sim.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            for _ in range(args.sweep_steps):
+                sim.step_async(sub)
+            ev1.record(stream)
+            ev1.synchronize()
+            sim.synchronize()
+            frame_ms = ev0.elapsed_time(ev1) / args.sweep_steps
+            counts_, _ = sim.read_friends(slots=1)
+            nl, nd = float(counts_[:, 0].mean()), float(counts_[:, 1].mean())
+            sim.enable_stage_timing(True)
+            totals: dict[str, float] = {}
+            for _ in range(3):
+                sim.Step(sub)
+                for k, v in sim.stage_timings().items():
+                    totals[k] = totals.get(k, 0.0) + v / 3.0
+            sim.close()
+            launches = {"computeScaling": iters * sub, "computeDelta": iters * sub}
+            groups = {}
+            for g, names in SWEEP_GROUPS.items():
+                ms = sum(totals.get(k, 0.0) for k in names)
+                byts = 0.0
+                for k in names:
+                    if k in STAGE_BYTES:
+                        byts += STAGE_BYTES[k](nl, nd) * n * launches.get(k, sub)
+                    elif k == "radixsort":
+                        byts += (16.0 * 3 + 4.0) * n * sub  # 3 passes of 8-bit digits
+                groups[g] = {"ms_per_step": round(ms, 4), "gb_per_s": byts / (ms / 1e3) / 1e9 if ms else None,
+                             "hbm_frac": (byts / (ms / 1e3) / 1e9) / peak if ms else None}
+            line = {"sweep": "double_dam_break", "particles": n, "iterations": iters,
+                    "value": n * iters * sub / (frame_ms / 1e3), "unit": UNIT, "ms_per_step": frame_ms,
+                    "steps": args.sweep_steps, "warmup": args.sweep_warmup, "neighbours": {"density_pass": nl,
+                    "other_passes": nd}, "groups": groups, "peak_gbs": peak, "peak_source": peak_kind}
+            print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -332,7 +393,14 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sweep", action="store_true", help="particle-count sweep (double dam break) instead")
+    ap.add_argument("--sweep-counts", default="262144,2097152,8388608")
+    ap.add_argument("--sweep-steps", type=int, default=20)
+    ap.add_argument("--sweep-warmup", type=int, default=10)
     args = ap.parse_args()
+    if args.sweep:
+        sweep(args)
+        return
     if args.impl == "gb300":
         args.warmup = max(3, args.warmup)  # at least 3 untimed frames
     if args.impl == "reference":

@@ -227,6 +227,13 @@ int pbf_scene_block(int nx, int ny, int nz, float spacing,
                     float ox, float oy, float oz,
                     float jitter, uint64_t seed, float* pos);
 
+/* Double dam break for the particle-count sweep: n particles in two 1:2:1
+   blocks on the floor of opposite corners of a 2:1:1 box whose volume is
+   n * spacing^3 / fill.  pos receives n float4 records; box receives xMin,
+   xMax, yMin, yMax, zMin, zMax. */
+int pbf_scene_double_dam_break(int n, float spacing, float fill, float jitter, uint64_t seed,
+                               float* pos, float* box);
+
 #ifdef __cplusplus
 }
 #endif

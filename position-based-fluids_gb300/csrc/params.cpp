@@ -143,3 +143,43 @@ extern "C" int pbf_scene_block(int nx, int ny, int nz, float spacing, float ox, 
             }
     return PBF_OK;
 }
+
+// Double dam break: two blocks of n/2 particles each (the second takes the
+// odd one), aspect 1:2:1 in x:y:z, standing on the floor in opposite x/z
+// corners of a 2:1:1 box whose volume is n * spacing^3 / fill.  Each block is
+// a lattice of a x 2a x a sites with a the smallest integer holding its
+// particles, filled x fastest, then z, then y, so only its top layer can be
+// partial.  Jitter as in pbf_scene_block (one std::mt19937_64 stream for both
+// blocks).  box receives xMin, xMax, yMin, yMax, zMin, zMax.
+extern "C" int pbf_scene_double_dam_break(int n, float spacing, float fill, float jitter, uint64_t seed,
+                                          float* pos, float* box) {
+    if (!pos || !box || n < 2 || !(spacing > 0.0f) || !(fill > 0.0f) || !(fill <= 1.0f))
+        return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_scene_double_dam_break: bad arguments");
+    const double s = spacing;
+    const double side = std::cbrt((double)n * s * s * s / fill / 2.0);  // box is 2*side x side x side
+    const double bx[6] = {0.0, 2.0 * side, 0.0, side, 0.0, side};
+    for (int k = 0; k < 6; ++k) box[k] = (float)bx[k];
+    std::mt19937_64 rng(seed);
+    size_t out = 0;
+    for (int b = 0; b < 2; ++b) {
+        const int count = b == 0 ? n / 2 : n - n / 2;
+        int a = 1;
+        while ((long long)a * (2 * a) * a < count) ++a;
+        // block 0 at the low x/z corner, block 1 at the high one, half a spacing from the walls
+        const double ox = b == 0 ? 0.5 * s : bx[1] - (a - 0.5) * s;
+        const double oz = b == 0 ? 0.5 * s : bx[5] - (a - 0.5) * s;
+        const double oy = 0.5 * s;
+        int placed = 0;
+        for (int iy = 0; iy < 2 * a && placed < count; ++iy)
+            for (int iz = 0; iz < a && placed < count; ++iz)
+                for (int ix = 0; ix < a && placed < count; ++ix, ++placed, ++out) {
+                    const double o[3] = {ox + ix * s, oy + iy * s, oz + iz * s};
+                    for (int c = 0; c < 3; ++c) {
+                        const double u = (double)(rng() >> 11) * 0x1.0p-53;
+                        pos[4 * out + c] = (float)(o[c] + (2.0 * u - 1.0) * jitter);
+                    }
+                    pos[4 * out + 3] = 0.0f;
+                }
+    }
+    return PBF_OK;
+}

@@ -105,6 +105,7 @@ def library() -> ctypes.CDLL:
         "pbf_reference_lattice": [P, f32p],
         "pbf_scene_block": [c_int, c_int, c_int, c_float, c_float, c_float, c_float, c_float, c_uint64, f32p],
         "pbf_sort_state_noalloc": [P, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+        "pbf_scene_double_dam_break": [c_int, c_float, c_float, c_float, c_uint64, f32p, f32p],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -338,7 +339,7 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_step", "pbf_step_async", "pbf_synchronize", "pbf_read_state", "pbf_write_state",
         "pbf_device_positions", "pbf_get_stream", "pbf_sort_state", "pbf_read_friends",
         "pbf_enable_stage_timing", "pbf_stage_timings", "pbf_launch_count", "pbf_use_graph",
-        "pbf_reference_lattice", "pbf_scene_block", "pbf_sort_state_noalloc",
+        "pbf_reference_lattice", "pbf_scene_block", "pbf_sort_state_noalloc", "pbf_scene_double_dam_break",
     ])
 
 
@@ -358,4 +359,28 @@ def make_scene(name: str):
     pos = scene_block(*spec["block"], spec["spacing"], spec["origin"], spec["jitter"], spec["seed"])
     if pos.shape[0] != params.particleCount:
         raise ValueError(f"scene {name}: block holds {pos.shape[0]} particles, .par says {params.particleCount}")
+    return params, pos, np.zeros_like(pos)
+
+
+def grid_size_for_box(box, h: float) -> int:
+    """Smallest power-of-two hash size holding the Morton number of every cell
+    of the box (so that the modulo never merges two cells of the box)."""
+    import math
+    cells = [max(1, int(math.ceil((box[2 * k + 1] - box[2 * k]) / h))) for k in range(3)]
+    bits = [max(1, int(math.ceil(math.log2(c)))) if c > 1 else 1 for c in cells]
+    top = max(3 * bits[0] - 3, 3 * bits[1] - 2, 3 * bits[2] - 1) + 1  # highest Morton bit + 1
+    return 1 << top
+
+
+def make_double_dam_break(n: int, iterations: int = 4, seed: int = 20240601, fill: float = 0.25):
+    """(params, pos, vel) of the particle-count sweep's double dam break: the
+    dam_break_1m solver settings in a box sized for a 25 % fill."""
+    params = load_scenario("dam_break_1m")
+    pos = np.zeros((n, 4), np.float32)
+    box = np.zeros(6, np.float32)
+    _check(library().pbf_scene_double_dam_break(n, 0.05, fill, 0.005, seed, _f32(pos), _f32(box)))
+    params.particleCount = n
+    params.simIterations = iterations
+    params.xMin, params.xMax, params.yMin, params.yMax, params.zMin, params.zMax = (float(b) for b in box)
+    params.gridBufSize = grid_size_for_box(box, params.h)
     return params, pos, np.zeros_like(pos)
