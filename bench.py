@@ -382,6 +382,65 @@ def sweep(args) -> None:
             print(json.dumps(line), flush=True)
 
 
+def batched(args) -> None:
+    """256 independent dam breaks (pbf.make_batch_scenes) advanced together,
+    each substep one CUDA graph over all scenes with autotuned block sizes;
+    compared with the same scenes run one at a time on the plain path and
+    with the single-scene 1M dam break."""
+    import numpy as np
+    import torch
+    import pbf
+
+    def rate(sim, n, frames, warm):
+        sub = int(sim.params.subSteps)
+        stream = torch.cuda.ExternalStream(sim.stream())
+        for _ in range(warm):
+            sim.step_async(sub)
+        sim.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(frames):
+            sim.step_async(sub)
+        e1.record(stream)
+        e1.synchronize()
+        sim.synchronize()
+        ms = e0.elapsed_time(e1) / frames
+        return n * int(sim.params.simIterations) * sub / (ms / 1e3), ms
+
+    scenes, positions = pbf.make_batch_scenes(count=args.batch_scenes)
+    pos = np.concatenate(positions)
+    total = int(pos.shape[0])
+    sim = pbf.Simulation.create(scenes, pos, np.zeros_like(pos), device=0)
+    for _ in range(args.warmup):
+        sim.step_async(int(sim.params.subSteps))
+    sim.synchronize()
+    blocks = sim.autotune(trial_substeps=2)
+    launches0 = sim.launch_count()
+    batch_rate, batch_ms = rate(sim, total, args.steps, 0)
+    launches = sim.launch_count() - launches0
+    sim.close()
+    seq_ms = 0.0
+    for p, x in zip(scenes, positions):
+        one = pbf.Simulation.create(p, x, np.zeros_like(x), device=0)
+        _, ms = rate(one, int(p.particleCount), args.batch_seq_steps, 3)
+        seq_ms += ms
+        one.close()
+    seq_rate = total * int(scenes[0].simIterations) * int(scenes[0].subSteps) / (seq_ms / 1e3)
+    params, p1, v1 = pbf.make_scene(SCENE)
+    single = pbf.Simulation.create(params, p1, v1, device=0)
+    single_rate, _ = rate(single, int(params.particleCount), args.steps, args.warmup)
+    single.close()
+    line = {"batched": f"{len(scenes)} dam-break scenes", "particles": total, "value": batch_rate, "unit": UNIT,
+            "ms_per_step": batch_ms, "steps": args.steps, "warmup": args.warmup, "gpu_launches": int(launches),
+            "autotuned_blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity"], blocks)),
+            "sequential_value": seq_rate, "ratio_vs_sequential": batch_rate / seq_rate,
+            "single_scene_value": single_rate, "ratio_vs_single_scene": batch_rate / single_rate,
+            "config": {"scenes": len(scenes), "counts": "log-uniform in [4096, 65536], seed 7",
+                       "fill": 0.3, "tilt_deg": "U(0, 10)", "xsph_c": "U(0.005, 0.05)", "iterations": 4,
+                       "substeps_per_step": 2, "cuda_graph": True}}
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -397,7 +456,13 @@ def main() -> None:
     ap.add_argument("--sweep-counts", default="262144,2097152,8388608")
     ap.add_argument("--sweep-steps", type=int, default=20)
     ap.add_argument("--sweep-warmup", type=int, default=10)
+    ap.add_argument("--batched", action="store_true", help="256 batched scenes instead")
+    ap.add_argument("--batch-scenes", type=int, default=256)
+    ap.add_argument("--batch-seq-steps", type=int, default=10)
     args = ap.parse_args()
+    if args.batched:
+        batched(args)
+        return
     if args.sweep:
         sweep(args)
         return

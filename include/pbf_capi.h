@@ -213,6 +213,37 @@ int pbf_use_graph(pbf_ctx* ctx, int enable);
 int pbf_sort_state_noalloc(const PbfParameters* params, const float* d_pred,
                            uint32_t* d_keys, uint32_t* d_perm, uint32_t* d_cells, void* stream);
 
+/* ------------------------------------------------------------- batches -- */
+
+/* A context that advances `nscenes` independent scenes together, every stage
+   one launch over all of them (no counterpart in the reference, which runs one
+   scene).  scenes[s] describes scene s; the scenes must agree on every field
+   except particleCount, the box (xMin..zMax), the gravity (garvity or the
+   gravity vector) and viscosityFactor.  The particle arrays of the other calls
+   are the scenes' arrays concatenated in order (pbf_scene_offsets gives the
+   boundaries); each scene's particles stay inside its range across steps and
+   its results are bit-identical to running it alone with the same
+   gridBufSize.  InitBuffers with init_pos == NULL places each scene's
+   reference lattice. */
+int pbf_create_batch(const PbfParameters* scenes, int nscenes, int device, pbf_ctx** out);
+
+/* offsets[s] .. offsets[s+1] is scene s's index range (nscenes + 1 words; a
+   single-scene context reports 0 and particleCount). */
+int pbf_scene_offsets(pbf_ctx* ctx, uint32_t* offsets);
+
+/* ------------------------------------------------------------ autotuner -- */
+
+/* Threads per block of the five neighbour kernels, in the order friends,
+   density (scaling), delta, viscosity, vorticity.  Results do not depend on
+   them; set requires multiples of 32 in [32, 512]. */
+int pbf_get_launch_shape(pbf_ctx* ctx, int* blocks);
+int pbf_set_launch_shape(pbf_ctx* ctx, const int* blocks);
+
+/* Time `trial_substeps` substeps from the current state for each candidate
+   block size (64, 128, 256, 512), keep the fastest per kernel, restore the
+   state, and report the choice through blocks_out (5 ints, may be NULL). */
+int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out);
+
 /* ------------------------------------------------------------- scenarios -- */
 
 /* The reference's initial lattice (Simulation::CreateParticles,

@@ -54,6 +54,13 @@ struct pbf_ctx {
     uint32_t cellsWords = 0;  // gridBufSize the cell table was allocated for
     int listSlots = 0;
 
+    // batch: scene s owns particles [sceneOffsets[s], sceneOffsets[s+1])
+    std::vector<PbfParameters> sceneParams;  // empty for a single scene
+    std::vector<uint32_t> sceneOffsets;
+    pbf::SceneParams* scenes = nullptr;      // device table, batches only
+    uint16_t* sceneOf = nullptr;             // device, batches only
+    pbf::LaunchShape shape;
+
     pbf::SortPlan plan;
     pbf::DevConsts consts{};
     int curPos = 0, curVel = 0, curPred = 1, keysIdx = 0;
@@ -160,6 +167,16 @@ DevConsts make_consts(const PbfParameters& p, int n) {
     return c;
 }
 
+SceneParams make_scene_params(const PbfParameters& p, uint32_t keyBase) {
+    const DevConsts c = make_consts(p, 0);
+    SceneParams s{};
+    s.gx = c.gx; s.gy = c.gy; s.gz = c.gz;
+    for (int k = 0; k < 3; ++k) { s.lo[k] = c.lo[k]; s.hi[k] = c.hi[k]; }
+    s.visc = c.visc;
+    s.keyBase = keyBase;
+    return s;
+}
+
 }  // namespace pbf
 
 namespace {
@@ -203,6 +220,30 @@ int validate(pbf_ctx* ctx, const PbfParameters& p) {
     if (!(p.h > 0.0f) || !(p.timeStep > 0.0f))
         return fail(ctx, PBF_ERR_INVALID, "SmoothLen and TimeStep must be positive");
     if (p.simIterations > 1000) return fail(ctx, PBF_ERR_INVALID, "simIterations must be <= 1000");
+    return PBF_OK;
+}
+
+bool is_batch(const pbf_ctx* ctx) { return !ctx->sceneParams.empty(); }
+
+pbf::Batch batch_of(const pbf_ctx* ctx) { return pbf::Batch{ctx->scenes, ctx->sceneOf}; }
+
+// Scenes of a batch share every parameter but the particle count, the box,
+// the gravity and the XSPH factor.
+int check_batch_compatible(pbf_ctx* ctx, const std::vector<PbfParameters>& sp) {
+    const PbfParameters& a = sp[0];
+    for (size_t s = 1; s < sp.size(); ++s) {
+        const PbfParameters& b = sp[s];
+        const bool same = a.timeStep == b.timeStep && a.simIterations == b.simIterations && a.subSteps == b.subSteps &&
+                          a.h == b.h && a.h_2 == b.h_2 && a.restDensity == b.restDensity && a.epsilon == b.epsilon &&
+                          a.vorticityFactor == b.vorticityFactor && a.surfaceTenstionK == b.surfaceTenstionK &&
+                          a.surfaceTenstionDist == b.surfaceTenstionDist && a.friendsCircles == b.friendsCircles &&
+                          a.particlesPerCircle == b.particlesPerCircle && a.gridBufSize == b.gridBufSize &&
+                          a.boxClamp == b.boxClamp && a.zeroDistanceGuard == b.zeroDistanceGuard;
+        if (!same)
+            return fail(ctx, PBF_ERR_INVALID,
+                        "scene " + std::to_string(s) + " differs from scene 0 in a parameter scenes must share "
+                        "(only particleCount, the box, gravity and viscosityFactor may differ)");
+    }
     return PBF_OK;
 }
 
@@ -256,7 +297,9 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
     auto mark = [&](const char* name) { return clock ? clock->stage(name) : PBF_OK; };
 
     mark("predictPositions");
-    pbf::launch_predict_keys(c, ctx->pos[P], ctx->vel[V], ctx->pred[0], ctx->keys[0], ctx->perm[0], paused, s);
+    const pbf::Batch b = batch_of(ctx);
+    const pbf::LaunchShape& ls = ctx->shape;
+    pbf::launch_predict_keys(c, b, ctx->pos[P], ctx->vel[V], ctx->pred[0], ctx->keys[0], ctx->perm[0], paused, s);
     ++launched;
     int sortedPos = P, sortedPred = 0;
     if (!paused) {
@@ -275,7 +318,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
     mark("updateCells");
     pbf::launch_update_cells(c.n, keys, ctx->cells, s);
     mark("buildFriendsList");
-    pbf::launch_build_friends(c, ctx->pred[sortedPred], ctx->cells, ctx->list, ctx->meta, ctx->errWord, s);
+    pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, ctx->list, ctx->meta, ctx->errWord, ls.friends, s);
     mark("resetPartList");
     pbf::launch_reset_cells(c.n, keys, ctx->cells, s);
     launched += 3;
@@ -283,10 +326,10 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
     const unsigned iters = ctx->params.simIterations;
     for (unsigned it = 0; it < iters; ++it) {
         mark("computeScaling");
-        pbf::launch_compute_scaling(c, ctx->pred[a], ctx->pred[a ^ 1], ctx->density, ctx->list, ctx->meta, s);
+        pbf::launch_compute_scaling(c, ctx->pred[a], ctx->pred[a ^ 1], ctx->density, ctx->list, ctx->meta, ls.scaling, s);
         mark("computeDelta");
-        pbf::launch_compute_delta(c, ctx->pred[a ^ 1], ctx->pred[a], ctx->density, ctx->list, ctx->meta,
-                                  it + 1 == iters, s);
+        pbf::launch_compute_delta(c, b, ctx->pred[a ^ 1], ctx->pred[a], ctx->density, ctx->list, ctx->meta,
+                                  it + 1 == iters, ls.delta, s);
         launched += 2;
     }
     if (iters == 0) {  // packData with the density buffer as it stands (src/Simulation.cpp:591)
@@ -297,9 +340,11 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
     mark("updateVelocities");
     pbf::launch_update_velocities(c, ctx->pred[a], ctx->pos[sortedPos], ctx->pos[sortedPos ^ 1], ctx->vel[V], s);
     mark("applyViscosity");
-    pbf::launch_apply_viscosity(c, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], ctx->omega, ctx->list, ctx->meta, s);
+    pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], ctx->omega, ctx->list, ctx->meta,
+                                ls.viscosity, s);
     mark("applyVorticity");
-    pbf::launch_apply_vorticity(c, ctx->pred[a], ctx->omega, ctx->vel[V ^ 1], ctx->vel[V], ctx->list, ctx->meta, s);
+    pbf::launch_apply_vorticity(c, ctx->pred[a], ctx->omega, ctx->vel[V ^ 1], ctx->vel[V], ctx->list, ctx->meta,
+                                ls.vorticity, s);
     launched += 3;
     PBF_CUDA(ctx, cudaGetLastError());
     ctx->curPos = sortedPos ^ 1;
@@ -359,6 +404,38 @@ const char* pbf_last_error(const pbf_ctx* ctx) {
     return ctx ? ctx->lastError.c_str() : pbf::tls_error.c_str();
 }
 
+int pbf_create_batch(const PbfParameters* scenes, int nscenes, int device, pbf_ctx** out) {
+    if (!scenes || !out || nscenes < 1) return fail(nullptr, PBF_ERR_INVALID, "pbf_create_batch: bad arguments");
+    if (nscenes > 65535) return fail(nullptr, PBF_ERR_INVALID, "pbf_create_batch: at most 65535 scenes");
+    std::vector<PbfParameters> sp(scenes, scenes + nscenes);
+    if (int rc = check_batch_compatible(nullptr, sp)) return rc;
+    uint64_t total = 0;
+    for (const auto& p : sp) {
+        if (p.particleCount < 1) return fail(nullptr, PBF_ERR_INVALID, "pbf_create_batch: a scene has no particles");
+        total += p.particleCount;
+    }
+    if (total > PBF_MAX_PARTICLES) return fail(nullptr, PBF_ERR_INVALID, "pbf_create_batch: more than 2^26 particles in all");
+    if ((uint64_t)nscenes * sp[0].gridBufSize > (1ull << 28))
+        return fail(nullptr, PBF_ERR_INVALID, "pbf_create_batch: scenes x gridBufSize must be <= 2^28");
+    PbfParameters merged = sp[0];
+    merged.particleCount = (unsigned)total;
+    int rc = pbf_create(&merged, device, out);
+    if (rc) return rc;
+    if (nscenes > 1) {
+        (*out)->sceneParams = sp;
+        (*out)->sceneOffsets.assign(1, 0u);
+        for (const auto& p : sp) (*out)->sceneOffsets.push_back((*out)->sceneOffsets.back() + p.particleCount);
+    }
+    return PBF_OK;
+}
+
+int pbf_scene_offsets(pbf_ctx* ctx, uint32_t* offsets) {
+    if (!ctx || !offsets) return fail(ctx, PBF_ERR_INVALID, "pbf_scene_offsets: NULL argument");
+    if (!is_batch(ctx)) { offsets[0] = 0; offsets[1] = ctx->params.particleCount; return PBF_OK; }
+    std::copy(ctx->sceneOffsets.begin(), ctx->sceneOffsets.end(), offsets);
+    return PBF_OK;
+}
+
 int pbf_create(const PbfParameters* params, int device, pbf_ctx** out) {
     if (!params || !out) return fail(nullptr, PBF_ERR_INVALID, "pbf_create: NULL argument");
     *out = nullptr;
@@ -389,6 +466,7 @@ int pbf_destroy(pbf_ctx* ctx) {
     }
     dev_free(ctx->omega); dev_free(ctx->density); dev_free(ctx->hist); dev_free(ctx->cells);
     dev_free(ctx->list); dev_free(ctx->meta); dev_free(ctx->errWord);
+    dev_free(ctx->scenes); dev_free(ctx->sceneOf);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PBF_OK;
@@ -421,8 +499,21 @@ int pbf_init_buffers(pbf_ctx* ctx, const float* init_pos, const float* init_vel)
     const float* src = init_pos;
     if (!src) {
         host.assign(4 * (size_t)n, 0.0f);
-        if ((rc = pbf_reference_lattice(&p, host.data())) != PBF_OK) return fail(ctx, rc, pbf_last_error(nullptr));
+        if (is_batch(ctx)) {
+            for (size_t s = 0; s < ctx->sceneParams.size(); ++s)
+                if ((rc = pbf_reference_lattice(&ctx->sceneParams[s], host.data() + 4 * (size_t)ctx->sceneOffsets[s])))
+                    return fail(ctx, rc, pbf_last_error(nullptr));
+        } else if ((rc = pbf_reference_lattice(&p, host.data())) != PBF_OK) {
+            return fail(ctx, rc, pbf_last_error(nullptr));
+        }
         src = host.data();
+    }
+    if (is_batch(ctx)) {
+        std::vector<uint16_t> ids(n);
+        for (size_t s = 0; s + 1 < ctx->sceneOffsets.size(); ++s)
+            std::fill(ids.begin() + ctx->sceneOffsets[s], ids.begin() + ctx->sceneOffsets[s + 1], (uint16_t)s);
+        if ((rc = dev_alloc(ctx, &ctx->sceneOf, n))) return rc;
+        PBF_CUDA(ctx, cudaMemcpy(ctx->sceneOf, ids.data(), 2 * (size_t)n, cudaMemcpyHostToDevice));
     }
     PBF_CUDA(ctx, cudaMemcpy(ctx->pos[0], src, 16 * (size_t)n, cudaMemcpyHostToDevice));
     if (init_vel) PBF_CUDA(ctx, cudaMemcpy(ctx->vel[0], init_vel, 16 * (size_t)n, cudaMemcpyHostToDevice));
@@ -445,8 +536,9 @@ int pbf_init_cells(pbf_ctx* ctx) {
     PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     drop_graph(ctx);
     int rc;
-    if ((rc = dev_alloc(ctx, &ctx->cells, 2 * (size_t)p.gridBufSize))) return rc;
-    PBF_CUDA(ctx, cudaMemset(ctx->cells, 0xFF, 8 * (size_t)p.gridBufSize));
+    const size_t tableWords = (size_t)p.gridBufSize * (is_batch(ctx) ? ctx->sceneParams.size() : 1);
+    if ((rc = dev_alloc(ctx, &ctx->cells, 2 * tableWords))) return rc;
+    PBF_CUDA(ctx, cudaMemset(ctx->cells, 0xFF, 8 * tableWords));
     ctx->cellsWords = p.gridBufSize;
     ctx->listSlots = (int)(p.friendsCircles * p.particlesPerCircle);
     if ((rc = dev_alloc(ctx, &ctx->list, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->meta, ctx->n)))
@@ -476,7 +568,17 @@ int pbf_init_kernels(pbf_ctx* ctx) {
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
     drop_graph(ctx);
     ctx->consts = pbf::make_consts(ctx->params, ctx->n);
-    ctx->plan = pbf::make_sort_plan(ctx->n, ctx->params.gridBufSize);
+    uint64_t keyRange = ctx->params.gridBufSize;
+    if (is_batch(ctx)) {
+        const size_t S = ctx->sceneParams.size();
+        keyRange *= S;
+        std::vector<pbf::SceneParams> table(S);
+        for (size_t s = 0; s < S; ++s)
+            table[s] = pbf::make_scene_params(ctx->sceneParams[s], (uint32_t)(s * ctx->params.gridBufSize));
+        if ((rc = dev_alloc(ctx, &ctx->scenes, S))) return rc;
+        PBF_CUDA(ctx, cudaMemcpy(ctx->scenes, table.data(), sizeof(pbf::SceneParams) * S, cudaMemcpyHostToDevice));
+    }
+    ctx->plan = pbf::make_sort_plan(ctx->n, (uint32_t)keyRange);
     if (ctx->plan.histWords != ctx->histWords) {
         if ((rc = dev_alloc(ctx, &ctx->hist, ctx->plan.histWords))) return rc;
         ctx->histWords = ctx->plan.histWords;
@@ -487,6 +589,7 @@ int pbf_init_kernels(pbf_ctx* ctx) {
 
 int pbf_set_params(pbf_ctx* ctx, const PbfParameters* params) {
     if (!ctx || !params) return fail(ctx, PBF_ERR_INVALID, "pbf_set_params: NULL argument");
+    if (is_batch(ctx)) return fail(ctx, PBF_ERR_UNSUPPORTED, "pbf_set_params applies to single-scene contexts");
     int rc = validate(ctx, *params);
     if (rc) return rc;
     if (ctx->buffersReady && (int)params->particleCount != ctx->n)
@@ -590,7 +693,7 @@ int pbf_sort_state(pbf_ctx* ctx, const float* pred, uint32_t* keys, uint32_t* pe
     if (!pred) return fail(ctx, PBF_ERR_INVALID, "pbf_sort_state: pred is NULL");
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
     const int n = ctx->n;
-    const uint32_t grid = ctx->params.gridBufSize;
+    const uint32_t grid = (uint32_t)(ctx->params.gridBufSize * (is_batch(ctx) ? ctx->sceneParams.size() : 1));
     float4* dPred = nullptr;
     uint32_t *k[2] = {nullptr, nullptr}, *pm[2] = {nullptr, nullptr}, *dCells = nullptr, *dHist = nullptr;
     auto cleanup = [&] {
@@ -608,7 +711,7 @@ int pbf_sort_state(pbf_ctx* ctx, const float* pred, uint32_t* keys, uint32_t* pe
     cudaStream_t s = ctx->stream;
     cudaMemcpyAsync(dPred, pred, 16 * (size_t)n, cudaMemcpyHostToDevice, s);
     cudaMemsetAsync(dCells, 0xFF, 8 * (size_t)grid, s);
-    pbf::launch_compute_keys(ctx->consts, dPred, k[0], pm[0], s);
+    pbf::launch_compute_keys(ctx->consts, batch_of(ctx), dPred, k[0], pm[0], s);
     const int r = pbf::launch_radix_sort(ctx->plan, k, pm, dHist, nullptr, nullptr, nullptr, nullptr, s);
     pbf::launch_update_cells(n, k[r], dCells, s);
     const uint32_t nKeys = ((uint32_t)n + 2047u) / 2048u * 2048u;
@@ -687,6 +790,92 @@ int pbf_launch_count(pbf_ctx* ctx, uint64_t* count) {
     if (!ctx || !count) return fail(ctx, PBF_ERR_INVALID, "pbf_launch_count: NULL argument");
     *count = ctx->launches;
     return PBF_OK;
+}
+
+int pbf_get_launch_shape(pbf_ctx* ctx, int* blocks) {
+    if (!ctx || !blocks) return fail(ctx, PBF_ERR_INVALID, "pbf_get_launch_shape: NULL argument");
+    const pbf::LaunchShape& s = ctx->shape;
+    blocks[0] = s.friends; blocks[1] = s.scaling; blocks[2] = s.delta; blocks[3] = s.viscosity; blocks[4] = s.vorticity;
+    return PBF_OK;
+}
+
+int pbf_set_launch_shape(pbf_ctx* ctx, const int* blocks) {
+    if (!ctx || !blocks) return fail(ctx, PBF_ERR_INVALID, "pbf_set_launch_shape: NULL argument");
+    for (int k = 0; k < 5; ++k)
+        if (blocks[k] < 32 || blocks[k] > pbf::kMaxBlock || blocks[k] % 32)
+            return fail(ctx, PBF_ERR_INVALID, "block sizes must be multiples of 32 in [32, 512]");
+    ctx->shape.friends = blocks[0]; ctx->shape.scaling = blocks[1]; ctx->shape.delta = blocks[2];
+    ctx->shape.viscosity = blocks[3]; ctx->shape.vorticity = blocks[4];
+    drop_graph(ctx);
+    return PBF_OK;
+}
+
+// Times `trial_substeps` substeps from the current state with every candidate
+// block size and keeps, for each neighbour kernel, the fastest.  The state is
+// saved before and restored after every trial, so the simulation continues
+// from where it was; every block size gives bit-identical results.
+int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (trial_substeps < 1) return fail(ctx, PBF_ERR_INVALID, "pbf_autotune: trial_substeps must be >= 1");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const size_t n = (size_t)ctx->n;
+    float4 *savePos = nullptr, *saveVel = nullptr;
+    float* saveDensity = nullptr;
+    uint32_t* saveKeys = nullptr;
+    auto release = [&] { cudaFree(savePos); cudaFree(saveVel); cudaFree(saveDensity); cudaFree(saveKeys); };
+    if (cudaMalloc((void**)&savePos, 16 * n) || cudaMalloc((void**)&saveVel, 16 * n) ||
+        cudaMalloc((void**)&saveDensity, 4 * n) || cudaMalloc((void**)&saveKeys, 4 * n)) {
+        release();
+        return fail(ctx, PBF_ERR_CUDA, "pbf_autotune: cannot allocate the state copy");
+    }
+    const int pos0 = ctx->curPos, vel0 = ctx->curVel, pred0 = ctx->curPred, keys0 = ctx->keysIdx;
+    const bool stepped0 = ctx->stepped, timing0 = ctx->stageTiming;
+    const uint64_t launches0 = ctx->launches;
+    const pbf::LaunchShape shape0 = ctx->shape;
+    cudaMemcpyAsync(savePos, ctx->pos[pos0], 16 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(saveVel, ctx->vel[vel0], 16 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(saveDensity, ctx->density, 4 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(saveKeys, ctx->keys[keys0], 4 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    auto restore = [&] {
+        ctx->curPos = pos0; ctx->curVel = vel0; ctx->curPred = pred0; ctx->keysIdx = keys0;
+        cudaMemcpyAsync(ctx->pos[pos0], savePos, 16 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+        cudaMemcpyAsync(ctx->vel[vel0], saveVel, 16 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+        cudaMemcpyAsync(ctx->density, saveDensity, 4 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+        cudaMemcpyAsync(ctx->keys[keys0], saveKeys, 4 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    };
+    const char* names[5] = {"buildFriendsList", "computeScaling", "computeDelta", "applyViscosity", "applyVorticity"};
+    const int candidates[4] = {64, 128, 256, 512};
+    float best[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
+    int choice[5] = {256, 256, 256, 256, 256};
+    ctx->stageTiming = true;
+    for (int cand : candidates) {
+        ctx->shape = pbf::LaunchShape{cand, cand, cand, cand, cand};
+        ctx->stageNames.clear();
+        ctx->stageMs.clear();
+        StageClock clock{ctx, {}};
+        for (int k = 0; k < trial_substeps && rc == PBF_OK; ++k) rc = enqueue_substep(ctx, &clock);
+        if (rc == PBF_OK) rc = clock.finish();
+        restore();
+        if (rc != PBF_OK) break;
+        for (int q = 0; q < 5; ++q)
+            for (size_t k = 0; k < ctx->stageNames.size(); ++k)
+                if (ctx->stageNames[k] == names[q] && ctx->stageMs[k] < best[q]) { best[q] = ctx->stageMs[k]; choice[q] = cand; }
+    }
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    release();
+    ctx->stageTiming = timing0;
+    ctx->stageNames.clear();
+    ctx->stageMs.clear();
+    ctx->stepped = stepped0;
+    ctx->launches = launches0;
+    drop_graph(ctx);
+    if (rc != PBF_OK) { ctx->shape = shape0; return rc; }
+    if (e != cudaSuccess) { ctx->shape = shape0; return fail(ctx, PBF_ERR_CUDA, std::string("pbf_autotune: ") + cudaGetErrorString(e)); }
+    ctx->shape = pbf::LaunchShape{choice[0], choice[1], choice[2], choice[3], choice[4]};
+    if (blocks_out) for (int q = 0; q < 5; ++q) blocks_out[q] = choice[q];
+    return read_error_word(ctx);
 }
 
 int pbf_use_graph(pbf_ctx* ctx, int enable) {

@@ -35,26 +35,52 @@ int fail(pbf_ctx* ctx, int code, const std::string& msg);
 
 DevConsts make_consts(const PbfParameters& p, int n);
 
+// The values that may differ between the scenes of a batch.  A batch keeps
+// all scenes in one particle array; scene s owns a fixed index range (its
+// keys are offset by s * gridBufSize, so the stable sort never moves a
+// particle out of it) and sceneOf[i] names the scene of particle i.
+struct SceneParams {
+    float gx, gy, gz;
+    float lo[3], hi[3];
+    float visc;
+    uint32_t keyBase;  // s * gridBufSize
+    uint32_t pad;
+};
+// scenes == nullptr: a single scene whose values are those of DevConsts.
+struct Batch {
+    const SceneParams* scenes;
+    const uint16_t* sceneOf;
+};
+SceneParams make_scene_params(const PbfParameters& p, uint32_t keyBase);
+
+// Threads per block of the kernels whose block size the autotuner chooses.
+struct LaunchShape {
+    int friends = 256, scaling = 256, delta = 256, viscosity = 256, vorticity = 256;
+};
+constexpr int kMaxBlock = 512;
+
 // ---- kernels (pbf_kernels.cu) ----
-void launch_predict_keys(const DevConsts& c, const float4* pos, float4* vel, float4* pred,
+void launch_predict_keys(const DevConsts& c, Batch b, const float4* pos, float4* vel, float4* pred,
                          uint32_t* keys, uint32_t* perm, int paused, cudaStream_t s);
-void launch_compute_keys(const DevConsts& c, const float4* pred, uint32_t* keys, uint32_t* perm, cudaStream_t s);
+void launch_compute_keys(const DevConsts& c, Batch b, const float4* pred, uint32_t* keys, uint32_t* perm,
+                         cudaStream_t s);
 void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred,
                           float4* posOut, float4* predOut, cudaStream_t s);
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
-void launch_build_friends(const DevConsts& c, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint2* meta, int* errorWord, cudaStream_t s);
+void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
+                          uint2* meta, int* errorWord, int block, cudaStream_t s);
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
-                            const uint32_t* list, const uint2* meta, cudaStream_t s);
-void launch_compute_delta(const DevConsts& c, const float4* predPacked, float4* predOut, const float* density,
-                          const uint32_t* list, const uint2* meta, int lastIteration, cudaStream_t s);
+                            const uint32_t* list, const uint2* meta, int block, cudaStream_t s);
+void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, float4* predOut,
+                          const float* density, const uint32_t* list, const uint2* meta, int lastIteration,
+                          int block, cudaStream_t s);
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
                               float4* vel, cudaStream_t s);
-void launch_apply_viscosity(const DevConsts& c, const float4* pred, const float4* velIn, float4* velOut,
-                            float4* omega, const uint32_t* list, const uint2* meta, cudaStream_t s);
+void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
+                            float4* omega, const uint32_t* list, const uint2* meta, int block, cudaStream_t s);
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
-                            float4* velOut, const uint32_t* list, const uint2* meta, cudaStream_t s);
+                            float4* velOut, const uint32_t* list, const uint2* meta, int block, cudaStream_t s);
 
 // ---- radix sort (pbf_sort.cu) ----
 struct SortPlan {

@@ -35,7 +35,13 @@ namespace {
 constexpr uint32_t kEmpty = 0xFFFFFFFFu;  // END_OF_CELL_LIST
 constexpr int kBlock = 256;
 
-inline unsigned blocks_for(int n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+inline unsigned blocks_for(int n, int block = kBlock) { return (unsigned)((n + block - 1) / block); }
+
+// Scene values of particle i: from the batch table, or DevConsts for a
+// single scene.
+__device__ __forceinline__ uint32_t key_base(const Batch& b, int i) {
+    return b.scenes ? b.scenes[b.sceneOf[i]].keyBase : 0u;
+}
 
 // utilities.cl:69-77
 __device__ __forceinline__ uint32_t expand_bits(int xi) {
@@ -59,34 +65,41 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 
 // ------------------------------------------------------------- predict --
 // predict_positions.cl:8-17 fused with computeKeys (radixsort.cl:7-19).
-__global__ void predict_keys_kernel(DevConsts c, const float4* __restrict__ pos, float4* __restrict__ vel,
+__global__ void predict_keys_kernel(DevConsts c, Batch b, const float4* __restrict__ pos, float4* __restrict__ vel,
                                     float4* __restrict__ pred, uint32_t* __restrict__ keys,
                                     uint32_t* __restrict__ perm, int paused) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     float4 v = vel[i];
+    float gx = c.gx, gy = c.gy, gz = c.gz;
+    uint32_t base = 0;
+    if (b.scenes) {
+        const SceneParams& sp = b.scenes[b.sceneOf[i]];
+        gx = sp.gx; gy = sp.gy; gz = sp.gz;
+        base = sp.keyBase;
+    }
     if (!paused) {
-        v.x = v.x + c.dt * c.gx;
-        v.y = v.y + c.dt * c.gy;
-        v.z = v.z + c.dt * c.gz;
+        v.x = v.x + c.dt * gx;
+        v.y = v.y + c.dt * gy;
+        v.z = v.z + c.dt * gz;
         vel[i] = v;
     }
     const float4 p = pos[i];
     const float4 q = make_float4(p.x + c.dt * v.x, p.y + c.dt * v.y, p.z + c.dt * v.z, p.w + c.dt * v.w);
     pred[i] = q;
     if (!paused) {
-        keys[i] = grid_hash(__float2int_rz(q.x / c.h), __float2int_rz(q.y / c.h), __float2int_rz(q.z / c.h), c.grid);
+        keys[i] = base + grid_hash(__float2int_rz(q.x / c.h), __float2int_rz(q.y / c.h), __float2int_rz(q.z / c.h), c.grid);
         perm[i] = (uint32_t)i;
     }
 }
 
 // radixsort.cl:1-20 alone (keys of given predicted positions, no padding).
-__global__ void compute_keys_kernel(DevConsts c, const float4* __restrict__ pred, uint32_t* __restrict__ keys,
-                                    uint32_t* __restrict__ perm) {
+__global__ void compute_keys_kernel(DevConsts c, Batch b, const float4* __restrict__ pred,
+                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ perm) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     const float4 q = pred[i];
-    keys[i] = grid_hash(__float2int_rz(q.x / c.h), __float2int_rz(q.y / c.h), __float2int_rz(q.z / c.h), c.grid);
+    keys[i] = key_base(b, i) + grid_hash(__float2int_rz(q.x / c.h), __float2int_rz(q.y / c.h), __float2int_rz(q.z / c.h), c.grid);
     perm[i] = (uint32_t)i;
 }
 
@@ -159,8 +172,8 @@ __device__ __forceinline__ int circles_kept(uint64_t cnt, int C, int total, floa
 // formed from the three spread coordinates of each axis, and the circle is
 // read off precomputed r^2 thresholds (DevConsts::circT): the same integer
 // the sqrt / divide / cube / truncate sequence gives, without computing it.
-__global__ void __launch_bounds__(kBlock)
-build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* __restrict__ cells,
+__global__ void __launch_bounds__(kMaxBlock)
+build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const uint2* __restrict__ cells,
                      uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
@@ -173,6 +186,7 @@ build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* 
     const uint32_t exm = expand_bits(cx - 1), ex0 = expand_bits(cx), exp_ = expand_bits(cx + 1);
     const uint32_t eym = expand_bits(cy - 1) << 1, ey0 = expand_bits(cy) << 1, eyp = expand_bits(cy + 1) << 1;
     const uint32_t ezm = expand_bits(cz - 1) << 2, ez0 = expand_bits(cz) << 2, ezp = expand_bits(cz + 1) << 2;
+    const uint32_t base = key_base(b, i);
     uint64_t cnt = 0;  // 8 circles x 8-bit counters
     for (int x = -1; x <= 1; ++x) {
         const uint32_t ex = x < 0 ? exm : (x > 0 ? exp_ : ex0);
@@ -180,7 +194,7 @@ build_friends_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* 
             const uint32_t exy = ex | (y < 0 ? eym : (y > 0 ? eyp : ey0));
             for (int z = -1; z <= 1; ++z) {
                 const uint32_t m = exy | (z < 0 ? ezm : (z > 0 ? ezp : ez0));
-                const uint2 range = cells[pow2 ? (m & mask) : (m % c.grid)];
+                const uint2 range = cells[base + (pow2 ? (m & mask) : (m % c.grid))];
                 if (range.x == kEmpty) continue;
                 const uint32_t last = min(range.y, (uint32_t)(n - 1));
                 if (range.x > last) { atomicOr(err, 1); continue; }
@@ -268,7 +282,7 @@ __device__ __forceinline__ bool in_support(const DevConsts& c, float r2) {
 
 // -------------------------------------------------------------- scaling --
 // compute_scaling.cl:27-112 followed by pack_data.cl (w = lambda).
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxBlock)
 compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __restrict__ predPacked,
                        float* __restrict__ density, const uint32_t* __restrict__ list,
                        const uint2* __restrict__ meta) {
@@ -309,8 +323,8 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
 // the optional box clamp on `future`, then update_predicted.cl.  After the
 // last iteration w carries the density (pack_data.cl with the density source,
 // src/Simulation.cpp:591).
-__global__ void __launch_bounds__(kBlock)
-compute_delta_kernel(DevConsts c, const float4* __restrict__ pp, float4* __restrict__ predOut,
+__global__ void __launch_bounds__(kMaxBlock)
+compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, float4* __restrict__ predOut,
                      const float* __restrict__ density, const uint32_t* __restrict__ list,
                      const uint2* __restrict__ meta, int lastIteration) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -342,9 +356,16 @@ compute_delta_kernel(DevConsts c, const float4* __restrict__ pp, float4* __restr
     float fy = pi.y + (c.negGradSpiky * sy) / c.rho0;
     float fz = pi.z + (c.negGradSpiky * sz) / c.rho0;
     if (c.clamp) {
-        fx = fx < c.lo[0] ? c.lo[0] : (fx > c.hi[0] ? c.hi[0] : fx);
-        fy = fy < c.lo[1] ? c.lo[1] : (fy > c.hi[1] ? c.hi[1] : fy);
-        fz = fz < c.lo[2] ? c.lo[2] : (fz > c.hi[2] ? c.hi[2] : fz);
+        const float* lo = c.lo;
+        const float* hi = c.hi;
+        if (b.scenes) {
+            const SceneParams& sp = b.scenes[b.sceneOf[i]];
+            lo = sp.lo;
+            hi = sp.hi;
+        }
+        fx = fx < lo[0] ? lo[0] : (fx > hi[0] ? hi[0] : fx);
+        fy = fy < lo[1] ? lo[1] : (fy > hi[1] ? hi[1] : fy);
+        fz = fz < lo[2] ? lo[2] : (fz > hi[2] ? hi[2] : fz);
     }
     const float dx = fx - pi.x, dy = fy - pi.y, dz = fz - pi.z;
     predOut[i] = make_float4(pi.x + dx, pi.y + dy, pi.z + dz, lastIteration ? density[i] : pi.w + 0.0f);
@@ -368,8 +389,8 @@ __global__ void update_velocities_kernel(DevConsts c, const float4* __restrict__
 
 // apply_viscosity.cl:12-86, every neighbour read from the pre-pass
 // velocities (Jacobi).
-__global__ void __launch_bounds__(kBlock)
-apply_viscosity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ velIn,
+__global__ void __launch_bounds__(kMaxBlock)
+apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const float4* __restrict__ velIn,
                        float4* __restrict__ velOut, float4* __restrict__ omega,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -403,12 +424,13 @@ apply_viscosity_kernel(DevConsts c, const float4* __restrict__ pred, const float
     vsx = vsx * c.poly6;
     vsy = vsy * c.poly6;
     vsz = vsz * c.poly6;
-    velOut[i] = make_float4(vi.x + c.visc * vsx, vi.y + c.visc * vsy, vi.z + c.visc * vsz, vi.w + c.visc * 0.0f);
+    const float visc = b.scenes ? b.scenes[b.sceneOf[i]].visc : c.visc;
+    velOut[i] = make_float4(vi.x + visc * vsx, vi.y + visc * vsy, vi.z + visc * vsz, vi.w + visc * 0.0f);
     omega[i] = make_float4(ox * c.negGradSpiky, oy * c.negGradSpiky, oz * c.negGradSpiky, 0.0f);
 }
 
 // apply_vorticity.cl:12-86
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxBlock)
 apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
                        const float4* __restrict__ velIn, float4* __restrict__ velOut,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta) {
@@ -455,13 +477,14 @@ apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float
 }  // namespace
 
 // ------------------------------------------------------------- launchers --
-void launch_predict_keys(const DevConsts& c, const float4* pos, float4* vel, float4* pred, uint32_t* keys,
+void launch_predict_keys(const DevConsts& c, Batch b, const float4* pos, float4* vel, float4* pred, uint32_t* keys,
                          uint32_t* perm, int paused, cudaStream_t s) {
-    predict_keys_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pos, vel, pred, keys, perm, paused);
+    predict_keys_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, b, pos, vel, pred, keys, perm, paused);
 }
 
-void launch_compute_keys(const DevConsts& c, const float4* pred, uint32_t* keys, uint32_t* perm, cudaStream_t s) {
-    compute_keys_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, keys, perm);
+void launch_compute_keys(const DevConsts& c, Batch b, const float4* pred, uint32_t* keys, uint32_t* perm,
+                         cudaStream_t s) {
+    compute_keys_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, b, pred, keys, perm);
 }
 
 void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, float4* posOut,
@@ -477,21 +500,22 @@ void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream
     reset_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, reinterpret_cast<uint2*>(cells));
 }
 
-void launch_build_friends(const DevConsts& c, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint2* meta, int* errorWord, cudaStream_t s) {
-    build_friends_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, reinterpret_cast<const uint2*>(cells), list,
-                                                            meta, errorWord);
+void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
+                          uint2* meta, int* errorWord, int block, cudaStream_t s) {
+    build_friends_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, reinterpret_cast<const uint2*>(cells),
+                                                                  list, meta, errorWord);
 }
 
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
-                            const uint32_t* list, const uint2* meta, cudaStream_t s) {
-    compute_scaling_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, predPacked, density, list, meta);
+                            const uint32_t* list, const uint2* meta, int block, cudaStream_t s) {
+    compute_scaling_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, predPacked, density, list, meta);
 }
 
-void launch_compute_delta(const DevConsts& c, const float4* predPacked, float4* predOut, const float* density,
-                          const uint32_t* list, const uint2* meta, int lastIteration, cudaStream_t s) {
-    compute_delta_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, predPacked, predOut, density, list, meta,
-                                                            lastIteration);
+void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, float4* predOut,
+                          const float* density, const uint32_t* list, const uint2* meta, int lastIteration,
+                          int block, cudaStream_t s) {
+    compute_delta_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, b, predPacked, predOut, density, list, meta,
+                                                                  lastIteration);
 }
 
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
@@ -499,14 +523,14 @@ void launch_update_velocities(const DevConsts& c, const float4* pred, const floa
     update_velocities_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, posIn, posOut, vel);
 }
 
-void launch_apply_viscosity(const DevConsts& c, const float4* pred, const float4* velIn, float4* velOut,
-                            float4* omega, const uint32_t* list, const uint2* meta, cudaStream_t s) {
-    apply_viscosity_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, velIn, velOut, omega, list, meta);
+void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
+                            float4* omega, const uint32_t* list, const uint2* meta, int block, cudaStream_t s) {
+    apply_viscosity_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, velIn, velOut, omega, list, meta);
 }
 
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
-                            float4* velOut, const uint32_t* list, const uint2* meta, cudaStream_t s) {
-    apply_vorticity_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, omega, velIn, velOut, list, meta);
+                            float4* velOut, const uint32_t* list, const uint2* meta, int block, cudaStream_t s) {
+    apply_vorticity_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta);
 }
 
 }  // namespace pbf

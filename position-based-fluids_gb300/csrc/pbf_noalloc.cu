@@ -88,7 +88,7 @@ extern "C" int pbf_sort_state_noalloc(const PbfParameters* params, const float* 
     uint32_t* perm[2] = {d_perm, scratch + kMaxKeys};
     uint32_t* hist = scratch + 2 * kMaxKeys;
 
-    pbf::launch_compute_keys(c, reinterpret_cast<const float4*>(d_pred), keys[0], perm[0], s);
+    pbf::launch_compute_keys(c, pbf::Batch{nullptr, nullptr}, reinterpret_cast<const float4*>(d_pred), keys[0], perm[0], s);
     const int r = pbf::launch_radix_sort(plan, keys, perm, hist, nullptr, nullptr, nullptr, nullptr, s);
     cudaError_t e = cudaSuccess;
     if (r == 1) {  // an odd number of passes left the result in the scratch half

@@ -106,6 +106,11 @@ def library() -> ctypes.CDLL:
         "pbf_scene_block": [c_int, c_int, c_int, c_float, c_float, c_float, c_float, c_float, c_uint64, f32p],
         "pbf_sort_state_noalloc": [P, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
         "pbf_scene_double_dam_break": [c_int, c_float, c_float, c_float, c_uint64, f32p, f32p],
+        "pbf_create_batch": [P, c_int, c_int, POINTER(c_void_p)],
+        "pbf_scene_offsets": [c_void_p, u32p],
+        "pbf_get_launch_shape": [c_void_p, POINTER(c_int)],
+        "pbf_set_launch_shape": [c_void_p, POINTER(c_int)],
+        "pbf_autotune": [c_void_p, c_int, POINTER(c_int)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -175,11 +180,20 @@ def reference_lattice(params: PbfParameters) -> np.ndarray:
 class Simulation:
     """The reference's Simulation over the C-ABI, on one CUDA device."""
 
-    def __init__(self, params: PbfParameters, device: int = 0):
+    def __init__(self, params, device: int = 0):
+        """`params`: one PbfParameters, or a list of them for a batch of scenes."""
         self.lib = library()
-        self.params = params.copy()
         self._ctx = c_void_p()
-        _check(self.lib.pbf_create(ctypes.byref(self.params), device, ctypes.byref(self._ctx)))
+        if isinstance(params, (list, tuple)):
+            arr = (PbfParameters * len(params))(*[p.copy() for p in params])
+            _check(self.lib.pbf_create_batch(arr, len(params), device, ctypes.byref(self._ctx)))
+            self.scene_params = [p.copy() for p in params]
+            self.params = params[0].copy()
+            self.params.particleCount = sum(int(p.particleCount) for p in params)
+        else:
+            self.scene_params = None
+            self.params = params.copy()
+            _check(self.lib.pbf_create(ctypes.byref(self.params), device, ctypes.byref(self._ctx)))
 
     # -- lifetime ----------------------------------------------------------
     def close(self) -> None:
@@ -331,6 +345,26 @@ class Simulation:
     def use_graph(self, on: bool) -> None:
         _check(self.lib.pbf_use_graph(self._ctx, int(on)), self._ctx)
 
+    def scene_offsets(self) -> np.ndarray:
+        k = len(self.scene_params) if self.scene_params else 1
+        out = np.zeros(k + 1, np.uint32)
+        _check(self.lib.pbf_scene_offsets(self._ctx, _u32(out)), self._ctx)
+        return out
+
+    def launch_shape(self) -> list:
+        b = (c_int * 5)()
+        _check(self.lib.pbf_get_launch_shape(self._ctx, b), self._ctx)
+        return list(b)
+
+    def set_launch_shape(self, blocks) -> None:
+        b = (c_int * 5)(*blocks)
+        _check(self.lib.pbf_set_launch_shape(self._ctx, b), self._ctx)
+
+    def autotune(self, trial_substeps: int = 2) -> list:
+        b = (c_int * 5)()
+        _check(self.lib.pbf_autotune(self._ctx, trial_substeps, b), self._ctx)
+        return list(b)
+
 
 EXPORTED_SYMBOLS = sorted(
     ["pbf_last_error"] + [
@@ -340,6 +374,7 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_device_positions", "pbf_get_stream", "pbf_sort_state", "pbf_read_friends",
         "pbf_enable_stage_timing", "pbf_stage_timings", "pbf_launch_count", "pbf_use_graph",
         "pbf_reference_lattice", "pbf_scene_block", "pbf_sort_state_noalloc", "pbf_scene_double_dam_break",
+        "pbf_create_batch", "pbf_scene_offsets", "pbf_get_launch_shape", "pbf_set_launch_shape", "pbf_autotune",
     ])
 
 
@@ -384,3 +419,48 @@ def make_double_dam_break(n: int, iterations: int = 4, seed: int = 20240601, fil
     params.xMin, params.xMax, params.yMin, params.yMax, params.zMin, params.zMax = (float(b) for b in box)
     params.gridBufSize = grid_size_for_box(box, params.h)
     return params, pos, np.zeros_like(pos)
+
+
+def make_batch_scenes(count: int = 256, seed: int = 7, fill: float = 0.3, first: int | None = None):
+    """Scenes of the batched benchmark: `count` dam breaks with particle counts
+    drawn log-uniformly in [4096, 65536] (numpy PCG64 with `seed`); scene s is
+    a block of n_s particles (a cubic lattice of a^3 >= n_s sites at spacing
+    0.05, x fastest, cut at n_s) in the low corner of a 2:1:1 box of volume
+    n_s * 0.05^3 / fill, with gravity 9.8 tilted by
+    U(0, 10) degrees about a random horizontal axis and XSPH c ~ U(0.005, 0.05)
+    (viscosityFactor = c / 6378, the reference's XSPH omitting 1/rho_j).
+    All scenes share one gridBufSize, the largest any of them needs.
+    Returns (list of PbfParameters, list of pos arrays).  `first` keeps only
+    the first scenes of the same draw."""
+    import math
+    rng = np.random.default_rng(seed)
+    counts = np.rint(np.exp(rng.uniform(math.log(4096), math.log(65536), count))).astype(int)
+    tilt = np.radians(rng.uniform(0.0, 10.0, count))
+    phi = rng.uniform(0.0, 2.0 * math.pi, count)
+    cvis = rng.uniform(0.005, 0.05, count)
+    base = load_scenario("dam_break_1m")
+    scenes, positions = [], []
+    for s in range(count):
+        n = int(counts[s])
+        side = (n * 0.05 ** 3 / fill / 2.0) ** (1.0 / 3.0)
+        a = 1
+        while a * a * a < n:
+            a += 1
+        pos = scene_block(a, a, a, 0.05, (0.025, 0.025, 0.025), 0.005, seed * 1000003 + s)[:n].copy()
+        p = base.copy()
+        p.particleCount = n
+        p.xMin, p.xMax, p.yMin, p.yMax, p.zMin, p.zMax = 0.0, 2.0 * side, 0.0, side, 0.0, side
+        g = 9.8
+        p.gravityVectorEnable = 1
+        p.gravityX = g * math.sin(tilt[s]) * math.sin(phi[s])
+        p.gravityY = -g * math.cos(tilt[s])
+        p.gravityZ = -g * math.sin(tilt[s]) * math.cos(phi[s])
+        p.viscosityFactor = float(cvis[s] / 6378.0)
+        scenes.append(p)
+        positions.append(pos)
+    grid = max(grid_size_for_box([q.xMin, q.xMax, q.yMin, q.yMax, q.zMin, q.zMax], q.h) for q in scenes)
+    for q in scenes:
+        q.gridBufSize = grid
+    if first is not None:
+        scenes, positions = scenes[:first], positions[:first]
+    return scenes, positions
