@@ -214,6 +214,7 @@ def gpu_arm(args) -> None:
     for _ in range(args.warmup):
         sim.step_async(sub)
     sim.synchronize()
+    blocks = sim.autotune(trial_substeps=2) if not args.no_autotune else sim.launch_shape()
 
     # ---- timed region: K frames, state resident in HBM ----
     barrier()
@@ -300,7 +301,8 @@ def gpu_arm(args) -> None:
                    "particles": n, "iterations": iters, "substeps_per_step": sub,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "working set larger than L2 (no flush)", "mode": "reference-exact FP32 (no FMA contraction)",
-                   "cuda_graph": True},
+                   "cuda_graph": True,
+                   "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity"], blocks))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
                 "steps": e2e_steps},
         "gpu_launches": int(launches),
@@ -452,6 +454,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default block sizes")
     ap.add_argument("--sweep", action="store_true", help="particle-count sweep (double dam break) instead")
     ap.add_argument("--sweep-counts", default="262144,2097152,8388608")
     ap.add_argument("--sweep-steps", type=int, default=20)
