@@ -443,6 +443,84 @@ def batched(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def rollout(args) -> None:
+    """Differentiable rollout: the 65,536-particle dam break (64x32x32
+    block) for 60 frames of 2 substeps, checkpoints every 10 substeps.  Loss:
+    MSE between the final positions and those of a target run with gravity
+    tilted 5 degrees and XSPH c = 0.03.  Times pbf_rollout_forward and
+    pbf_rollout_backward (which recomputes each segment from its checkpoint
+    before running the adjoint kernels over it) with CUDA events on the
+    simulation's stream, next to the plain path's 120 substeps."""
+    import numpy as np
+    import torch
+    import pbf
+
+    frames, every = args.rollout_frames, args.rollout_every
+    params, pos, vel = pbf.make_rollout_scene(64, 32, 32)
+    n = int(params.particleCount)
+    substeps = frames * int(params.subSteps)
+    tparams = pbf.rollout_target_params(params)
+    with pbf.Simulation.create(tparams, pos, vel, device=0) as tsim:
+        tsim.Step(substeps)
+        target = tsim.positions_by_id().astype(np.float64)
+    sim = pbf.Simulation.create(params, pos, vel, device=0)
+    stream = torch.cuda.ExternalStream(sim.stream())
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    def dl_dx(x):
+        g = np.zeros((n, 4), np.float32)
+        g[:, :3] = (2.0 * (x[:, :3].astype(np.float64) - target[:, :3]) / (3.0 * n)).astype(np.float32)
+        return g
+
+    fwd, bwd, plain = [], [], []
+    launches = 0
+    blocks = sim.launch_shape()
+    for rep in range(args.warmup_rollouts + args.rollouts):
+        sim.write_state(pos, vel)
+        _, ms_plain = timed(lambda: sim.Step(substeps))
+        sim.write_state(pos, vel)
+        l0 = sim.launch_count()
+        _, ms_f = timed(lambda: sim.rollout_forward(substeps, every))
+        x = sim.positions_by_id()
+        loss = float(np.mean((x[:, :3].astype(np.float64) - target[:, :3]) ** 2))
+        g = dl_dx(x)
+        (dv, dc, dg), ms_b = timed(lambda: sim.rollout_backward(g))
+        if rep + 1 == args.warmup_rollouts and not args.no_autotune:
+            blocks = sim.autotune(trial_substeps=4)
+        if rep >= args.warmup_rollouts:
+            fwd.append(ms_f)
+            bwd.append(ms_b)
+            plain.append(ms_plain)
+            launches = sim.launch_count() - l0
+    sim.close()
+    f, bk, pl = float(np.median(fwd)), float(np.median(bwd)), float(np.median(plain))
+    list_bytes = 4 * n * int(params.friendsCircles) * int(params.particlesPerCircle)
+    tape_bytes = every * (4 * n + list_bytes + 8 * n + 16 * n * (int(params.simIterations) + 3)
+                          + (n * int(params.simIterations) if params.boxClamp else 0))
+    line = {"rollout": f"{n}-particle dam break (64x32x32), {frames} frames x {int(params.subSteps)} substeps",
+            "metric": "backward / forward time", "value": bk / f, "higher_is_better": False,
+            "forward_ms": f, "backward_ms": bk, "plain_steps_ms": pl,
+            "forward_us_per_substep": 1e3 * f / substeps, "backward_us_per_substep": 1e3 * bk / substeps,
+            "rollouts": args.rollouts, "warmup": args.warmup_rollouts, "gpu_launches": int(launches),
+            "forward_blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity"], blocks)),
+            "loss": loss, "grad_norms": {"v0": float(np.linalg.norm(dv[:, :3])), "c": float(dc),
+                                         "g": [float(v) for v in dg]},
+            "memory_bytes": {"tape_one_segment": tape_bytes, "checkpoints": (substeps // every + 1) * 36 * n},
+            "dtype": "f32",
+            "config": {"particles": n, "substeps": substeps, "checkpoint_every": every, "iterations":
+                       int(params.simIterations), "target": "gravity tilted 5 deg, XSPH c = 0.03",
+                       "gradients": "initial velocities, XSPH c, gravity vector"}}
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -462,7 +540,15 @@ def main() -> None:
     ap.add_argument("--batched", action="store_true", help="256 batched scenes instead")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-seq-steps", type=int, default=10)
+    ap.add_argument("--rollout", action="store_true", help="differentiable rollout forward/backward instead")
+    ap.add_argument("--rollout-frames", type=int, default=60)
+    ap.add_argument("--rollout-every", type=int, default=10)
+    ap.add_argument("--rollouts", type=int, default=3)
+    ap.add_argument("--warmup-rollouts", type=int, default=1)
     args = ap.parse_args()
+    if args.rollout:
+        rollout(args)
+        return
     if args.batched:
         batched(args)
         return

@@ -129,7 +129,9 @@ int pbf_synchronize(pbf_ctx* ctx);
    Replaces reading the GL-shared position buffers the renderer draws. */
 int pbf_read_state(pbf_ctx* ctx, float* pos, float* vel, float* pred);
 
-/* Overwrite positions and velocities from host memory (either may be NULL). */
+/* Overwrite positions and velocities from host memory (either may be NULL).
+   Writing positions renumbers the particles: record k becomes particle k
+   (pbf_read_ids). */
 int pbf_write_state(pbf_ctx* ctx, const float* pos, const float* vel);
 
 /* Device address of the current positions (float4 x particleCount), valid
@@ -230,6 +232,29 @@ int pbf_create_batch(const PbfParameters* scenes, int nscenes, int device, pbf_c
 /* offsets[s] .. offsets[s+1] is scene s's index range (nscenes + 1 words; a
    single-scene context reports 0 and particleCount). */
 int pbf_scene_offsets(pbf_ctx* ctx, uint32_t* offsets);
+
+/* ------------------------------------------------------------ rollouts -- */
+
+/* Original index (0 .. N-1 at InitBuffers) of each particle record in the
+   current order; the sort permutes the records every substep. */
+int pbf_read_ids(pbf_ctx* ctx, uint32_t* ids);
+
+/* Differentiable rollout (no counterpart in the reference).  Run `substeps`
+   substeps from the current state, keeping the state every
+   `checkpoint_every` substeps (and at the end) so that the reverse pass can
+   recompute each segment instead of storing every substep. */
+int pbf_rollout_forward(pbf_ctx* ctx, int substeps, int checkpoint_every);
+
+/* Reverse pass of the last pbf_rollout_forward, over a fixed neighbour
+   structure (each substep's sort permutation, friend lists and box-clamp
+   decisions are constants of the derivative; recomputing a segment from its
+   checkpoint reproduces them exactly).  dL_dx: adjoint of the final positions
+   (4 floats per particle, indexed by original particle index, w ignored).
+   Outputs (any may be NULL): dL_dv0 (4 per particle, by original index) for
+   the initial velocities, dL_dvisc for viscosityFactor, dL_dg (3) for the
+   gravity vector.  Memory: one segment of intermediate values.  The context's
+   state is left at the end of the rollout. */
+int pbf_rollout_backward(pbf_ctx* ctx, const float* dL_dx, float* dL_dv0, float* dL_dvisc, float* dL_dg);
 
 /* ------------------------------------------------------------ autotuner -- */
 

@@ -42,6 +42,14 @@ def lib() -> ctypes.CDLL:
         l.oracle_grid_hash.restype = c_uint32
         for f in (l.oracle_step_f32, l.oracle_step_f64, l.oracle_sort_f32, l.oracle_constants, l.oracle_max_threads):
             f.restype = c_int
+        l.oracle_rollout_record.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_int, c_void_p, c_int]
+        l.oracle_rollout_record.restype = c_void_p
+        l.oracle_rollout_free.argtypes = [c_void_p]
+        l.oracle_rollout_replay_f64.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+        l.oracle_rollout_replay_f64.restype = c_double
+        l.oracle_rollout_grad_f64.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                              c_void_p]
+        l.oracle_rollout_grad_f64.restype = c_double
         _lib = l
     return _lib
 
@@ -159,3 +167,60 @@ def ref_sort(params, pred):
     if rc != 0:
         raise ValueError(f"ref_sort_f32 rejected the input ({rc})")
     return keys, perm, cells
+
+
+class Rollout:
+    """A rollout over a fixed neighbour structure: the FP32 forward (identical
+    to the CUDA path) records the structure; replay() / grad() evaluate the
+    same function with that structure frozen, in FP64."""
+
+    def __init__(self, params, pos, vel, substeps, threads=0):
+        n = int(params.particleCount)
+        self.params = params
+        self.n = n
+        self.pos0 = np.array(pos, np.float32).reshape(n, 4)
+        self.vel0 = np.array(vel, np.float32).reshape(n, 4)
+        p = self.pos0.copy()
+        v = self.vel0.copy()
+        self.ids = np.zeros(n, np.uint32)
+        self.handle = lib().oracle_rollout_record(ctypes.byref(params), n, _ptr(p), _ptr(v), substeps, _ptr(self.ids), threads)
+        if not self.handle:
+            raise ValueError("oracle_rollout_record rejected the input")
+        self.pos_final32 = p  # final FP32 state, sorted order
+        self.vel_final32 = v
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            lib().oracle_rollout_free(self.handle)
+            self.handle = None
+
+    def final_by_id32(self):
+        out = np.zeros_like(self.pos_final32)
+        out[self.ids] = self.pos_final32
+        return out
+
+    def replay(self, vel0=None, gravity=None, visc=None, target=None):
+        """(loss, final positions by id) in FP64; gravity (3) / visc override the recorded values."""
+        v0 = np.ascontiguousarray(self.vel0 if vel0 is None else vel0, np.float64)
+        p0 = np.ascontiguousarray(self.pos0, np.float64)
+        out = np.zeros((self.n, 4), np.float64)
+        tgt = None if target is None else np.ascontiguousarray(target, np.float64)
+        g = None if gravity is None else np.ascontiguousarray(gravity, np.float64)
+        vc = None if visc is None else c_double(visc)
+        loss = lib().oracle_rollout_replay_f64(self.handle, _ptr(g), None if vc is None else ctypes.byref(vc),
+                                               _ptr(p0), _ptr(v0), _ptr(tgt), _ptr(out))
+        return loss, out
+
+    def grad(self, target, vel0=None, gravity=None, visc=None):
+        """(loss, dL/dv0 [n,4], dL/dviscosityFactor, dL/dgravity [3]) in FP64."""
+        v0 = np.ascontiguousarray(self.vel0 if vel0 is None else vel0, np.float64)
+        p0 = np.ascontiguousarray(self.pos0, np.float64)
+        tgt = np.ascontiguousarray(target, np.float64)
+        g = None if gravity is None else np.ascontiguousarray(gravity, np.float64)
+        vc = None if visc is None else c_double(visc)
+        dv = np.zeros((self.n, 4), np.float64)
+        dc = c_double(0)
+        dg = np.zeros(3, np.float64)
+        loss = lib().oracle_rollout_grad_f64(self.handle, _ptr(g), None if vc is None else ctypes.byref(vc), _ptr(p0),
+                                             _ptr(v0), _ptr(tgt), _ptr(dv), ctypes.byref(dc), _ptr(dg))
+        return loss, dv, dc.value, dg

@@ -326,7 +326,9 @@ template <typename T> void compute_scaling(State<T>& s, const Consts<T>& c) {
 // compute_delta.cl:54-185 (with the force planes the identity), then
 // update_predicted.cl (pred += delta).  The clamp, when enabled, bounds
 // `future` to the box before the delta is formed.
-template <typename T> void compute_delta(State<T>& s, const Consts<T>& c) {
+// `mask` (may be NULL): per particle, which coordinates the clamp moved, two
+// bits per axis (1: to the lower bound, 2: to the upper bound).
+template <typename T> void compute_delta(State<T>& s, const Consts<T>& c, uint8_t* mask = nullptr) {
     const int C = c.circles, P = c.perCircle;
     const T negG = -c.gradSpiky;
 #pragma omp parallel for schedule(dynamic, 256)
@@ -356,9 +358,17 @@ template <typename T> void compute_delta(State<T>& s, const Consts<T>& c) {
         V3<T> dp = {(negG * sum.x) / c.rho0, (negG * sum.y) / c.rho0, (negG * sum.z) / c.rho0};
         V3<T> fut = {pi.x + dp.x, pi.y + dp.y, pi.z + dp.z};
         if (c.clamp) {  // comparisons, so that -0.0 and NaN pass through unchanged
+            if (mask) {
+                T* f = &fut.x;
+                uint8_t m = 0;
+                for (int k = 0; k < 3; ++k) m |= (uint8_t)((f[k] < c.lo[k] ? 1 : (f[k] > c.hi[k] ? 2 : 0)) << (2 * k));
+                mask[i] = m;
+            }
             fut.x = fut.x < c.lo[0] ? c.lo[0] : (fut.x > c.hi[0] ? c.hi[0] : fut.x);
             fut.y = fut.y < c.lo[1] ? c.lo[1] : (fut.y > c.hi[1] ? c.hi[1] : fut.y);
             fut.z = fut.z < c.lo[2] ? c.lo[2] : (fut.z > c.hi[2] ? c.hi[2] : fut.z);
+        } else if (mask) {
+            mask[i] = 0;
         }
         V3<T> delta = {fut.x - pi.x, fut.y - pi.y, fut.z - pi.z};
         s.pred[i] = {pi.x + delta.x, pi.y + delta.y, pi.z + delta.z, pi.w + (T)0};
@@ -545,6 +555,410 @@ int run_steps(const PbfParameters* p, int n, T* pos, T* vel, T* pred, int subste
     return 0;
 }
 
+
+// ============================================================ rollouts ==
+// Gradients of a rollout over a fixed neighbour structure.  An FP32 forward
+// (identical to the pipeline above) records, per substep, the sort
+// permutation, the friend lists and which coordinates the box clamp moved.
+// The same function with that structure frozen is then evaluated in FP64
+// ("replay"), and its exact gradient is taken by reverse accumulation through
+// the substeps.  The replay is smooth in the inputs: the support test
+// r^2 < h^2 switches terms that vanish with their first derivative at r = h.
+
+struct Structure {
+    std::vector<uint32_t> perm;    // sorted index k came from index perm[k]
+    std::vector<int32_t> counts;   // N x C friends per circle
+    std::vector<int32_t> start;    // N + 1 offsets into list
+    std::vector<int32_t> list;     // the kept-for-density circles, circle-major
+    std::vector<uint8_t> mask;     // iterations x N clamp masks
+};
+
+struct RolloutRecord {
+    PbfParameters params;
+    int n = 0;
+    std::vector<Structure> steps;
+};
+
+template <typename T> struct Tape {
+    std::vector<V4<T>> xs;               // sorted positions before the update
+    std::vector<std::vector<V4<T>>> q;   // (p^t, lambda^t), t < iterations
+    std::vector<V4<T>> pI;               // final predictions, w = density of the last pass
+    std::vector<V4<T>> v2, omega;        // velocities before XSPH, vorticity
+};
+
+inline void kept_circles(const int32_t* cnt, int C, int& keptL, int& keptD) {
+    keptL = circles_kept(cnt, C, 0.6f);
+    keptD = circles_kept(cnt, C, 0.5f);
+}
+
+// Friends of i used by a pass keeping `kept` circles: list[start[i] .. +m).
+inline int kept_count(const int32_t* cnt, int kept) {
+    int m = 0;
+    for (int k = 0; k < kept; ++k) m += cnt[k];
+    return m;
+}
+
+// k(r) = (h - |r|)^2 r / |r| and the adjoint of its argument.
+template <typename T> inline V3<T> kvec(const V3<T>& r, T rl, T h) {
+    T hr = h - rl;
+    return {r.x / rl * hr * hr, r.y / rl * hr * hr, r.z / rl * hr * hr};
+}
+template <typename T> inline V3<T> kvec_adj(const V3<T>& r, T rl, T h, const V3<T>& kb) {
+    T f = (h - rl) * (h - rl) / rl;
+    T fp = -(h - rl) * (h + rl) / (rl * rl);
+    T s = fp * dot(kb, r) / rl;
+    return {f * kb.x + s * r.x, f * kb.y + s * r.y, f * kb.z + s * r.z};
+}
+
+template <typename T> inline bool support(const Consts<T>& c, T r2) { return r2 < c.h2 && (!c.guard || r2 > (T)0); }
+
+template <typename T> void atomic_add3(V4<T>& a, const V3<T>& v) {
+#pragma omp atomic
+    a.x += v.x;
+#pragma omp atomic
+    a.y += v.y;
+#pragma omp atomic
+    a.z += v.z;
+}
+
+// One substep of the frozen-structure function in T.  x, v: in/out (state in
+// the order of the previous substep on entry, sorted order on exit); ids
+// follows the permutation.  With a tape, the intermediate values are kept.
+template <typename T>
+void replay_substep(const Structure& st, const Consts<T>& c, int iters, std::vector<V4<T>>& x, std::vector<V4<T>>& v,
+                    std::vector<uint32_t>& ids, Tape<T>* tape) {
+    const int N = (int)x.size(), C = c.circles;
+    std::vector<V4<T>> p0(N), xs(N), p(N);
+    std::vector<uint32_t> ids2(N);
+    for (int i = 0; i < N; ++i) {
+        V4<T> v1 = {v[i].x + c.dt * c.gx, v[i].y + c.dt * c.gy, v[i].z + c.dt * c.gz, 0};
+        p0[i] = {x[i].x + c.dt * v1.x, x[i].y + c.dt * v1.y, x[i].z + c.dt * v1.z, 0};
+    }
+    for (int k = 0; k < N; ++k) { xs[k] = x[st.perm[k]]; p[k] = p0[st.perm[k]]; ids2[k] = ids[st.perm[k]]; }
+    ids.swap(ids2);
+    std::vector<T> lam(N), rho(N);
+    if (tape) { tape->xs = xs; tape->q.assign(iters, {}); }
+    const T negG = -c.gradSpiky;
+    for (int t = 0; t < iters; ++t) {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int i = 0; i < N; ++i) {
+            const int32_t* cnt = &st.counts[(size_t)i * C];
+            int kl, kd;
+            kept_circles(cnt, C, kl, kd);
+            const int m = kept_count(cnt, kl);
+            T ds = 0, gsk = 0;
+            V3<T> S = {0, 0, 0};
+            for (int f = 0; f < m; ++f) {
+                const int j = st.list[st.start[i] + f];
+                V3<T> r = sub(xyz(p[i]), xyz(p[j]));
+                T r2 = dot(r, r);
+                if (!support(c, r2)) continue;
+                T rl = std::sqrt(r2);
+                V3<T> g = scale(c.gradSpiky, kvec(r, rl, c.h));
+                T d = c.h2 - r2;
+                ds += d * d * d;
+                gsk += dot(g, g);
+                S = add(S, g);
+            }
+            rho[i] = ds * c.poly6;
+            T D = gsk + dot(S, S);
+            lam[i] = -(rho[i] / c.rho0 - 1) / (D / (c.rho0 * c.rho0) + c.eps);
+        }
+        if (tape) {
+            tape->q[t].resize(N);
+            for (int i = 0; i < N; ++i) tape->q[t][i] = {p[i].x, p[i].y, p[i].z, lam[i]};
+        }
+        std::vector<V4<T>> pn(N);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int i = 0; i < N; ++i) {
+            const int32_t* cnt = &st.counts[(size_t)i * C];
+            int kl, kd;
+            kept_circles(cnt, C, kl, kd);
+            const int m = kept_count(cnt, kd);
+            V3<T> sum = {0, 0, 0};
+            for (int f = 0; f < m; ++f) {
+                const int j = st.list[st.start[i] + f];
+                V3<T> r = sub(xyz(p[i]), xyz(p[j]));
+                T r2 = dot(r, r);
+                if (!support(c, r2)) continue;
+                T rl = std::sqrt(r2);
+                T W = (c.h2 - r2) * (c.h2 - r2) * (c.h2 - r2);
+                T rq = W / c.poly6q;
+                T a = lam[i] + lam[j] + c.K * rq * rq * rq * rq;
+                sum = add(sum, scale(a, kvec(r, rl, c.h)));
+            }
+            V3<T> fut = {p[i].x + negG * sum.x / c.rho0, p[i].y + negG * sum.y / c.rho0, p[i].z + negG * sum.z / c.rho0};
+            const uint8_t mk = st.mask[(size_t)t * N + i];
+            T* f = &fut.x;
+            for (int k = 0; k < 3; ++k) {
+                const int b = (mk >> (2 * k)) & 3;
+                if (b == 1) f[k] = c.lo[k];
+                else if (b == 2) f[k] = c.hi[k];
+            }
+            pn[i] = {fut.x, fut.y, fut.z, 0};
+        }
+        p.swap(pn);
+    }
+    std::vector<V4<T>> v2(N), v3(N), om(N);
+    for (int i = 0; i < N; ++i) {
+        v2[i] = {(p[i].x - xs[i].x) / c.dt, (p[i].y - xs[i].y) / c.dt, (p[i].z - xs[i].z) / c.dt, 0};
+        p[i].w = iters > 0 ? rho[i] : 0;
+    }
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < N; ++i) {
+        const int32_t* cnt = &st.counts[(size_t)i * C];
+        int kl, kd;
+        kept_circles(cnt, C, kl, kd);
+        const int m = kept_count(cnt, kd);
+        V3<T> vs = {0, 0, 0}, o = {0, 0, 0};
+        for (int f = 0; f < m; ++f) {
+            const int j = st.list[st.start[i] + f];
+            V3<T> r = sub(xyz(p[i]), xyz(p[j]));
+            T r2 = dot(r, r);
+            if (!support(c, r2) || !(std::fabs(p[j].w) > (T)1e-8f)) continue;
+            T rl = std::sqrt(r2);
+            V3<T> u = sub(xyz(v2[j]), xyz(v2[i]));
+            T d = c.h2 - r2;
+            vs = add(vs, scale(d * d * d, u));
+            o = add(o, cross(u, kvec(r, rl, c.h)));
+        }
+        v3[i] = {v2[i].x + c.visc * c.poly6 * vs.x, v2[i].y + c.visc * c.poly6 * vs.y, v2[i].z + c.visc * c.poly6 * vs.z, 0};
+        om[i] = {negG * o.x, negG * o.y, negG * o.z, 0};
+    }
+    std::vector<V4<T>> v4(N);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < N; ++i) {
+        const int32_t* cnt = &st.counts[(size_t)i * C];
+        int kl, kd;
+        kept_circles(cnt, C, kl, kd);
+        const int m = kept_count(cnt, kd);
+        V3<T> eta = {0, 0, 0};
+        for (int f = 0; f < m; ++f) {
+            const int j = st.list[st.start[i] + f];
+            V3<T> r = sub(xyz(p[i]), xyz(p[j]));
+            T r2 = dot(r, r);
+            if (!support(c, r2) || !(std::fabs(p[j].w) > (T)1e-8f)) continue;
+            T rl = std::sqrt(r2);
+            eta = add(eta, scale(fast_length(xyz(om[j])), kvec(r, rl, c.h)));
+        }
+        eta = scale(negG, eta);
+        T l = fast_length(eta);
+        V3<T> Nn = l > 0 ? scale((T)1 / l, eta) : V3<T>{0, 0, 0};
+        V3<T> fv = scale(c.vort * c.dt, cross(Nn, xyz(om[i])));
+        v4[i] = {v3[i].x + fv.x, v3[i].y + fv.y, v3[i].z + fv.z, 0};
+    }
+    if (tape) { tape->pI = p; tape->v2 = v2; tape->omega = om; }
+    x = p;
+    for (auto& q : x) q.w = 0;
+    v = v4;
+}
+
+// Reverse accumulation through one substep of the frozen-structure function.
+// xb, vb: adjoints of the substep's output (sorted order) on entry, of its
+// input (previous order) on exit.  cb, gb accumulate dL/d visc and dL/d g.
+template <typename T>
+void adjoint_substep(const Structure& st, const Consts<T>& c, int iters, const Tape<T>& tp, std::vector<V4<T>>& xb,
+                     std::vector<V4<T>>& vb, T& cb, T gb[3]) {
+    const int N = (int)xb.size(), C = c.circles;
+    const T negG = -c.gradSpiky, G = c.gradSpiky;
+    const std::vector<V4<T>>& p = tp.pI;
+    std::vector<V4<T>> pb(N, V4<T>{0, 0, 0, 0}), omb(N, V4<T>{0, 0, 0, 0}), v2b(N, V4<T>{0, 0, 0, 0});
+    // vorticity: v4 = v3 + dt*vort*(N x omega_i), N = eta/|eta|, eta = -G sum |om_j| k_ij
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < N; ++i) {
+        const int32_t* cnt = &st.counts[(size_t)i * C];
+        int kl, kd;
+        kept_circles(cnt, C, kl, kd);
+        const int m = kept_count(cnt, kd);
+        V3<T> eta = {0, 0, 0};
+        for (int f = 0; f < m; ++f) {
+            const int j = st.list[st.start[i] + f];
+            V3<T> r = sub(xyz(p[i]), xyz(p[j]));
+            T r2 = dot(r, r);
+            if (!support(c, r2) || !(std::fabs(p[j].w) > (T)1e-8f)) continue;
+            eta = add(eta, scale(fast_length(xyz(tp.omega[j])), kvec(r, std::sqrt(r2), c.h)));
+        }
+        eta = scale(negG, eta);
+        T l = fast_length(eta);
+        if (!(l > 0)) continue;
+        V3<T> Nn = scale((T)1 / l, eta);
+        V3<T> ub = scale(c.vort * c.dt, xyz(vb[i]));
+        V3<T> oi = xyz(tp.omega[i]);
+        V3<T> Nb = cross(oi, ub);
+        atomic_add3(omb[i], cross(ub, Nn));
+        V3<T> etab = scale((T)1 / l, sub(Nb, scale(dot(Nn, Nb), Nn)));
+        for (int f = 0; f < m; ++f) {
+            const int j = st.list[st.start[i] + f];
+            V3<T> r = sub(xyz(p[i]), xyz(p[j]));
+            T r2 = dot(r, r);
+            if (!support(c, r2) || !(std::fabs(p[j].w) > (T)1e-8f)) continue;
+            T rl = std::sqrt(r2);
+            V3<T> k = kvec(r, rl, c.h);
+            V3<T> oj = xyz(tp.omega[j]);
+            T ol = fast_length(oj);
+            if (ol > 0) atomic_add3(omb[j], scale(negG * dot(etab, k) / ol, oj));
+            V3<T> rb = kvec_adj(r, rl, c.h, scale(negG * ol, etab));
+            atomic_add3(pb[i], rb);
+            atomic_add3(pb[j], scale((T)-1, rb));
+        }
+    }
+    // XSPH + omega: v3 = v2 + visc*POLY6*sum (v2_j - v2_i) W_ij; omega = -G sum (v2_j - v2_i) x k_ij
+    T cacc = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : cacc)
+    for (int i = 0; i < N; ++i) {
+        const int32_t* cnt = &st.counts[(size_t)i * C];
+        int kl, kd;
+        kept_circles(cnt, C, kl, kd);
+        const int m = kept_count(cnt, kd);
+        V3<T> v3b = xyz(vb[i]), ob = xyz(omb[i]);
+        atomic_add3(v2b[i], v3b);
+        for (int f = 0; f < m; ++f) {
+            const int j = st.list[st.start[i] + f];
+            V3<T> r = sub(xyz(p[i]), xyz(p[j]));
+            T r2 = dot(r, r);
+            if (!support(c, r2) || !(std::fabs(p[j].w) > (T)1e-8f)) continue;
+            T rl = std::sqrt(r2);
+            V3<T> u = sub(xyz(tp.v2[j]), xyz(tp.v2[i]));
+            T d = c.h2 - r2;
+            T w = c.poly6 * d * d * d;
+            V3<T> k = kvec(r, rl, c.h);
+            cacc += w * dot(v3b, u);
+            V3<T> ub = add(scale(c.visc * w, v3b), scale(negG, cross(k, ob)));
+            atomic_add3(v2b[j], ub);
+            atomic_add3(v2b[i], scale((T)-1, ub));
+            T Wb = c.visc * c.poly6 * dot(v3b, u);
+            V3<T> rb = scale(Wb * (T)-6 * d * d, r);
+            rb = add(rb, kvec_adj(r, rl, c.h, scale(negG, cross(ob, u))));
+            atomic_add3(pb[i], rb);
+            atomic_add3(pb[j], scale((T)-1, rb));
+        }
+    }
+    cb += cacc;
+    // velocities: v2 = (p^I - xs)/dt, x' = p^I
+    std::vector<V4<T>> xsb(N);
+    for (int i = 0; i < N; ++i) {
+        pb[i] = {pb[i].x + xb[i].x + v2b[i].x / c.dt, pb[i].y + xb[i].y + v2b[i].y / c.dt,
+                 pb[i].z + xb[i].z + v2b[i].z / c.dt, 0};
+        xsb[i] = {-v2b[i].x / c.dt, -v2b[i].y / c.dt, -v2b[i].z / c.dt, 0};
+    }
+    // solver iterations, last first
+    for (int t = iters - 1; t >= 0; --t) {
+        const std::vector<V4<T>>& q = tp.q[t];
+        std::vector<V4<T>> pbt(N, V4<T>{0, 0, 0, 0});
+        std::vector<T> lb(N, 0);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int i = 0; i < N; ++i) {
+            V3<T> fb = xyz(pb[i]);
+            const uint8_t mk = st.mask[(size_t)t * N + i];
+            T* f = &fb.x;
+            for (int k = 0; k < 3; ++k)
+                if ((mk >> (2 * k)) & 3) f[k] = 0;
+            atomic_add3(pbt[i], fb);
+            const int32_t* cnt = &st.counts[(size_t)i * C];
+            int kl, kd;
+            kept_circles(cnt, C, kl, kd);
+            const int m = kept_count(cnt, kd);
+            for (int f2 = 0; f2 < m; ++f2) {
+                const int j = st.list[st.start[i] + f2];
+                V3<T> r = sub(xyz(q[i]), xyz(q[j]));
+                T r2 = dot(r, r);
+                if (!support(c, r2)) continue;
+                T rl = std::sqrt(r2);
+                T d = c.h2 - r2;
+                T W = d * d * d;
+                T rq = W / c.poly6q;
+                T a = q[i].w + q[j].w + c.K * rq * rq * rq * rq;
+                V3<T> k = kvec(r, rl, c.h);
+                T ab = negG / c.rho0 * dot(fb, k);
+#pragma omp atomic
+                lb[i] += ab;
+#pragma omp atomic
+                lb[j] += ab;
+                T sW = ab * (T)4 * c.K * rq * rq * rq / c.poly6q;
+                V3<T> rb = scale(sW * (T)-6 * d * d, r);
+                rb = add(rb, kvec_adj(r, rl, c.h, scale(negG / c.rho0 * a, fb)));
+                atomic_add3(pbt[i], rb);
+                atomic_add3(pbt[j], scale((T)-1, rb));
+            }
+        }
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int i = 0; i < N; ++i) {
+            const int32_t* cnt = &st.counts[(size_t)i * C];
+            int kl, kd;
+            kept_circles(cnt, C, kl, kd);
+            const int m = kept_count(cnt, kl);
+            T ds = 0, gsk = 0;
+            V3<T> S = {0, 0, 0};
+            for (int f = 0; f < m; ++f) {
+                const int j = st.list[st.start[i] + f];
+                V3<T> r = sub(xyz(q[i]), xyz(q[j]));
+                T r2 = dot(r, r);
+                if (!support(c, r2)) continue;
+                T rl = std::sqrt(r2);
+                V3<T> g = scale(G, kvec(r, rl, c.h));
+                T d = c.h2 - r2;
+                ds += d * d * d;
+                gsk += dot(g, g);
+                S = add(S, g);
+            }
+            T rho = ds * c.poly6, D = gsk + dot(S, S);
+            T den = D / (c.rho0 * c.rho0) + c.eps, Cc = rho / c.rho0 - 1;
+            T Cb = -lb[i] / den, Db = lb[i] * Cc / (den * den) / (c.rho0 * c.rho0);
+            T rhob = Cb / c.rho0;
+            for (int f = 0; f < m; ++f) {
+                const int j = st.list[st.start[i] + f];
+                V3<T> r = sub(xyz(q[i]), xyz(q[j]));
+                T r2 = dot(r, r);
+                if (!support(c, r2)) continue;
+                T rl = std::sqrt(r2);
+                T d = c.h2 - r2;
+                V3<T> g = scale(G, kvec(r, rl, c.h));
+                V3<T> rb = scale(rhob * c.poly6 * (T)-6 * d * d, r);
+                V3<T> gb = scale((T)2 * Db, add(g, S));
+                rb = add(rb, kvec_adj(r, rl, c.h, scale(G, gb)));
+                atomic_add3(pbt[i], rb);
+                atomic_add3(pbt[j], scale((T)-1, rb));
+            }
+        }
+        pb.swap(pbt);
+    }
+    // unsort, then predict: p0 = x + dt (v + dt g)
+    std::vector<V4<T>> xo(N), vo(N);
+    for (int k = 0; k < N; ++k) {
+        const uint32_t i = st.perm[k];
+        xo[i] = {xsb[k].x + pb[k].x, xsb[k].y + pb[k].y, xsb[k].z + pb[k].z, 0};
+        vo[i] = {c.dt * pb[k].x, c.dt * pb[k].y, c.dt * pb[k].z, 0};
+        gb[0] += c.dt * c.dt * pb[k].x;
+        gb[1] += c.dt * c.dt * pb[k].y;
+        gb[2] += c.dt * c.dt * pb[k].z;
+    }
+    xb.swap(xo);
+    vb.swap(vo);
+}
+
+Structure record_structure(const State<float>& s, const std::vector<uint8_t>& masks, int C) {
+    Structure st;
+    const int N = s.n;
+    st.perm.assign(s.perm.begin(), s.perm.begin() + N);
+    st.counts.assign(s.fcount.begin(), s.fcount.end());
+    st.start.assign(N + 1, 0);
+    const int P = (int)(s.friends.size() / ((size_t)N * C));
+    for (int i = 0; i < N; ++i) {
+        int kl, kd;
+        kept_circles(&s.fcount[(size_t)i * C], C, kl, kd);
+        st.start[i + 1] = st.start[i] + kept_count(&s.fcount[(size_t)i * C], kl);
+    }
+    st.list.resize(st.start[N]);
+    for (int i = 0; i < N; ++i) {
+        int kl, kd, o = st.start[i];
+        kept_circles(&s.fcount[(size_t)i * C], C, kl, kd);
+        for (int k = 0; k < kl; ++k)
+            for (int f = 0; f < s.fcount[(size_t)i * C + k]; ++f) st.list[o++] = s.friends[((size_t)i * C + k) * P + f];
+    }
+    st.mask = masks;
+    return st;
+}
+
 }  // namespace
 
 extern "C" {
@@ -599,6 +1013,134 @@ int oracle_constants(const PbfParameters* p, float* poly6, float* grad_spiky, fl
     if (grad_spiky) *grad_spiky = c.gradSpiky;
     if (poly6_q) *poly6_q = c.poly6q;
     return 0;
+}
+
+// ---- rollouts over a fixed neighbour structure ----
+
+// FP32 forward of `substeps` substeps (identical to oracle_step_f32),
+// recording the structure of each.  pos, vel: in/out; ids (n, may be NULL)
+// receives the original index of each final particle.  Returns a handle for
+// the replay / gradient calls (free with oracle_rollout_free), NULL on error.
+void* oracle_rollout_record(const PbfParameters* p, int n, float* pos, float* vel, int substeps, uint32_t* ids,
+                            int nthreads) {
+    if (check(p, n) || substeps < 1) return nullptr;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    Consts<float> c = make_consts<float>(*p);
+    auto* rec = new RolloutRecord();
+    rec->params = *p;
+    rec->n = n;
+    State<float> s;
+    s.n = n;
+    s.nKeys = int_ceil((uint32_t)n, 2048u);
+    s.pos.resize(n); s.vel.resize(n); s.pred.resize(n); s.predP.resize(n); s.omega.resize(n);
+    std::memcpy(s.pos.data(), pos, 16 * (size_t)n);
+    std::memcpy(s.vel.data(), vel, 16 * (size_t)n);
+    s.density.assign(n, 0); s.lambda.assign(n, 0);
+    s.keys.assign(s.nKeys, 0); s.perm.assign(s.nKeys, 0);
+    s.cells.assign(2 * (size_t)p->gridBufSize, kEmpty);
+    s.friends.assign((size_t)n * c.circles * c.perCircle, 0);
+    s.fcount.assign((size_t)n * c.circles, 0);
+    std::vector<uint32_t> idv(n);
+    for (int i = 0; i < n; ++i) idv[i] = (uint32_t)i;
+    std::vector<uint8_t> masks((size_t)p->simIterations * n, 0);
+    for (int step = 0; step < substeps; ++step) {
+        predict(s, c, false);
+        sort_particles(s, c);
+        std::vector<uint32_t> id2(n);
+        for (int k = 0; k < n; ++k) id2[k] = idv[s.perm[k]];
+        idv.swap(id2);
+        update_cells(s);
+        build_friends(s, c);
+        reset_grid(s);
+        for (unsigned it = 0; it < p->simIterations; ++it) {
+            compute_scaling(s, c);
+            compute_delta(s, c, masks.data() + (size_t)it * n);
+        }
+        update_velocities(s, c);
+        apply_viscosity(s, c);
+        apply_vorticity(s, c);
+        rec->steps.push_back(record_structure(s, masks, c.circles));
+    }
+    std::memcpy(pos, s.pos.data(), 16 * (size_t)n);
+    std::memcpy(vel, s.vel.data(), 16 * (size_t)n);
+    if (ids) std::memcpy(ids, idv.data(), 4 * (size_t)n);
+    return rec;
+}
+
+void oracle_rollout_free(void* handle) { delete static_cast<RolloutRecord*>(handle); }
+
+// The frozen-structure rollout in FP64 from pos0 / vel0 (4n doubles each,
+// original particle order) with gravity vector g (3 doubles) and
+// viscosityFactor *visc (NULL: the recorded values).  Writes the final positions by original
+// index to pos_by_id (4n, may be NULL) and returns the loss
+// mean_{i,axis} (x_final - target)^2 against target_by_id (4n, may be NULL).
+static Consts<double> replay_consts(const RolloutRecord& rec, const double* g, const double* visc) {
+    Consts<double> c = make_consts<double>(rec.params);
+    if (g) { c.gx = g[0]; c.gy = g[1]; c.gz = g[2]; }
+    if (visc) c.visc = *visc;
+    return c;
+}
+
+static double replay(const RolloutRecord& rec, const double* g, const double* visc, const double* pos0,
+                     const double* vel0, const double* target_by_id, double* pos_by_id,
+                     std::vector<Tape<double>>* tapes, std::vector<V4<double>>* xFinal,
+                     std::vector<uint32_t>* idsFinal) {
+    Consts<double> c = replay_consts(rec, g, visc);
+    const int n = rec.n;
+    std::vector<V4<double>> x(n), v(n);
+    std::memcpy(x.data(), pos0, 32 * (size_t)n);
+    std::memcpy(v.data(), vel0, 32 * (size_t)n);
+    std::vector<uint32_t> ids(n);
+    for (int i = 0; i < n; ++i) ids[i] = (uint32_t)i;
+    if (tapes) tapes->assign(rec.steps.size(), {});
+    for (size_t k = 0; k < rec.steps.size(); ++k)
+        replay_substep(rec.steps[k], c, (int)rec.params.simIterations, x, v, ids, tapes ? &(*tapes)[k] : nullptr);
+    double loss = 0;
+    for (int k = 0; k < n; ++k) {
+        const uint32_t id = ids[k];
+        if (pos_by_id) { pos_by_id[4 * id] = x[k].x; pos_by_id[4 * id + 1] = x[k].y; pos_by_id[4 * id + 2] = x[k].z; pos_by_id[4 * id + 3] = 0; }
+        if (target_by_id) {
+            const double* t = target_by_id + 4 * (size_t)id;
+            loss += (x[k].x - t[0]) * (x[k].x - t[0]) + (x[k].y - t[1]) * (x[k].y - t[1]) + (x[k].z - t[2]) * (x[k].z - t[2]);
+        }
+    }
+    if (xFinal) *xFinal = x;
+    if (idsFinal) *idsFinal = ids;
+    return loss / (3.0 * n);
+}
+
+double oracle_rollout_replay_f64(void* handle, const double* g, const double* visc, const double* pos0,
+                                 const double* vel0, const double* target_by_id, double* pos_by_id) {
+    return replay(*static_cast<RolloutRecord*>(handle), g, visc, pos0, vel0, target_by_id, pos_by_id, nullptr, nullptr,
+                  nullptr);
+}
+
+// Loss and its exact gradient (FP64) with respect to the initial velocities
+// (dv0, 4n doubles, original order), viscosityFactor (dvisc) and the gravity
+// vector (dg, 3 doubles), at gravity g / viscosityFactor *visc (NULL: as
+// recorded).
+double oracle_rollout_grad_f64(void* handle, const double* g, const double* visc, const double* pos0,
+                               const double* vel0, const double* target_by_id, double* dv0, double* dvisc, double* dg) {
+    const RolloutRecord& rec = *static_cast<RolloutRecord*>(handle);
+    std::vector<Tape<double>> tapes;
+    std::vector<V4<double>> x;
+    std::vector<uint32_t> ids;
+    const double loss = replay(rec, g, visc, pos0, vel0, target_by_id, nullptr, &tapes, &x, &ids);
+    Consts<double> c = replay_consts(rec, g, visc);
+    const int n = rec.n;
+    std::vector<V4<double>> xb(n), vb(n, V4<double>{0, 0, 0, 0});
+    for (int k = 0; k < n; ++k) {
+        const double* t = target_by_id + 4 * (size_t)ids[k];
+        const double s = 2.0 / (3.0 * n);
+        xb[k] = {s * (x[k].x - t[0]), s * (x[k].y - t[1]), s * (x[k].z - t[2]), 0};
+    }
+    double cb = 0, gb[3] = {0, 0, 0};
+    for (size_t k = rec.steps.size(); k-- > 0;)
+        adjoint_substep(rec.steps[k], c, (int)rec.params.simIterations, tapes[k], xb, vb, cb, gb);
+    if (dv0) std::memcpy(dv0, vb.data(), 32 * (size_t)n);
+    if (dvisc) *dvisc = cb;
+    if (dg) for (int k = 0; k < 3; ++k) dg[k] = gb[k];
+    return loss;
 }
 
 // Morton hash of one cell (utilities.cl:84-87).

@@ -35,6 +35,7 @@ CUDA_UNITS = {
     "pbf_sort.cu": [],
     "pbf_capi.cu": ["--fmad=false"],
     "pbf_noalloc.cu": ["--fmad=false"],
+    "pbf_adjoint.cu": [],
 }
 CXX_UNITS = ["params.cpp"]
 

@@ -58,6 +58,8 @@ struct pbf_ctx {
     std::vector<PbfParameters> sceneParams;  // empty for a single scene
     std::vector<uint32_t> sceneOffsets;
     pbf::SceneParams* scenes = nullptr;      // device table, batches only
+    uint32_t* ids = nullptr;                 // original index of each particle record
+    uint32_t* idsTmp = nullptr;
     uint16_t* sceneOf = nullptr;             // device, batches only
     pbf::LaunchShape shape;
 
@@ -75,6 +77,25 @@ struct pbf_ctx {
     bool stageTiming = false;
     std::vector<std::string> stageNames;
     std::vector<float> stageMs;
+
+    // rollout: state at the start of every segment of `rollEvery` substeps,
+    // and at the end (pbf_rollout_forward / pbf_rollout_backward)
+    struct Checkpoint {
+        float4* pos = nullptr;
+        float4* vel = nullptr;
+        uint32_t* ids = nullptr;
+        int curPos = 0, curVel = 0, curPred = 1, keysIdx = 0;
+    };
+    std::vector<Checkpoint> ckpt;
+    Checkpoint ckptEnd;
+    int rollSubsteps = 0, rollEvery = 0;
+    // reverse pass: one segment of tape plus the adjoint buffers, kept
+    // between calls while (rollEvery, simIterations, boxClamp) stay the same
+    std::vector<void*> tapeMem;
+    std::vector<pbf::AdjointTape> tapes;
+    pbf::AdjointBuffers adj{};
+    float4* adjById = nullptr;
+    int tapeEvery = 0, tapeIters = 0, tapeClamp = -1;
 };
 
 namespace pbf {
@@ -287,8 +308,10 @@ __global__ void pack_density_kernel(int n, float4* pred, const float* density) {
     if (i < n) pred[i].w = density[i];
 }
 
-// Enqueue one Simulation::Step on the context's stream.
-int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
+
+// Enqueue one Simulation::Step on the context's stream; with a tape, also
+// copy out what the reverse pass needs.
+int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tape = nullptr) {
     const pbf::DevConsts& c = ctx->consts;
     cudaStream_t s = ctx->stream;
     const int P = ctx->curPos, V = ctx->curVel;
@@ -308,28 +331,36 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
                                               nullptr, s);
         launched += pbf::radix_sort_launches(ctx->plan);
         mark("sortParticles");
-        pbf::launch_gather_sorted(c.n, ctx->perm[ctx->keysIdx], ctx->pos[P], ctx->pred[0], ctx->pos[P ^ 1],
-                                  ctx->pred[1], s);
+        pbf::launch_gather_sorted(c.n, ctx->perm[ctx->keysIdx], ctx->pos[P], ctx->pred[0], ctx->ids, ctx->pos[P ^ 1],
+                                  ctx->pred[1], ctx->idsTmp, s);
         ++launched;
         sortedPos = P ^ 1;
         sortedPred = 1;
     }
     const uint32_t* keys = ctx->keys[ctx->keysIdx];
+    const size_t v4 = 16 * (size_t)c.n;
+    // With a tape, the friend lists, the packed (p, lambda) of every
+    // iteration and omega are written straight into the tape's buffers.
+    uint32_t* list = tape ? tape->list : ctx->list;
+    uint2* meta = tape ? tape->meta : ctx->meta;
+    float4* omega = tape ? tape->omega : ctx->omega;
+    if (tape) cudaMemcpyAsync(tape->perm, ctx->perm[ctx->keysIdx], 4 * (size_t)c.n, cudaMemcpyDeviceToDevice, s);
     mark("updateCells");
     pbf::launch_update_cells(c.n, keys, ctx->cells, s);
     mark("buildFriendsList");
-    pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, ctx->list, ctx->meta, ctx->errWord, ls.friends, s);
+    pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, meta, ctx->errWord, ls.friends, s);
     mark("resetPartList");
     pbf::launch_reset_cells(c.n, keys, ctx->cells, s);
     launched += 3;
     int a = sortedPred;
     const unsigned iters = ctx->params.simIterations;
     for (unsigned it = 0; it < iters; ++it) {
+        float4* packed = tape ? tape->q[it] : ctx->pred[a ^ 1];
         mark("computeScaling");
-        pbf::launch_compute_scaling(c, ctx->pred[a], ctx->pred[a ^ 1], ctx->density, ctx->list, ctx->meta, ls.scaling, s);
+        pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, ls.scaling, s);
         mark("computeDelta");
-        pbf::launch_compute_delta(c, b, ctx->pred[a ^ 1], ctx->pred[a], ctx->density, ctx->list, ctx->meta,
-                                  it + 1 == iters, ls.delta, s);
+        pbf::launch_compute_delta(c, b, packed, ctx->pred[a], ctx->density, list, meta, it + 1 == iters,
+                                  tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr, ls.delta, s);
         launched += 2;
     }
     if (iters == 0) {  // packData with the density buffer as it stands (src/Simulation.cpp:591)
@@ -337,14 +368,15 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock) {
         pack_density_kernel<<<(c.n + 255) / 256, 256, 0, s>>>(c.n, ctx->pred[a], ctx->density);
         ++launched;
     }
+    if (tape) cudaMemcpyAsync(tape->pI, ctx->pred[a], v4, cudaMemcpyDeviceToDevice, s);
     mark("updateVelocities");
-    pbf::launch_update_velocities(c, ctx->pred[a], ctx->pos[sortedPos], ctx->pos[sortedPos ^ 1], ctx->vel[V], s);
+    pbf::launch_update_velocities(c, ctx->pred[a], ctx->pos[sortedPos], ctx->pos[sortedPos ^ 1], ctx->vel[V],
+                                  paused ? nullptr : ctx->idsTmp, ctx->ids, s);
+    if (tape) cudaMemcpyAsync(tape->v2, ctx->vel[V], v4, cudaMemcpyDeviceToDevice, s);
     mark("applyViscosity");
-    pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], ctx->omega, ctx->list, ctx->meta,
-                                ls.viscosity, s);
+    pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, ls.viscosity, s);
     mark("applyVorticity");
-    pbf::launch_apply_vorticity(c, ctx->pred[a], ctx->omega, ctx->vel[V ^ 1], ctx->vel[V], ctx->list, ctx->meta,
-                                ls.vorticity, s);
+    pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, ls.vorticity, s);
     launched += 3;
     PBF_CUDA(ctx, cudaGetLastError());
     ctx->curPos = sortedPos ^ 1;
@@ -395,6 +427,78 @@ int read_error_word(pbf_ctx* ctx) {
     return PBF_OK;
 }
 
+int save_checkpoint(pbf_ctx* ctx, pbf_ctx::Checkpoint& k) {
+    const size_t n = (size_t)ctx->n;
+    int rc;
+    if (!k.pos && ((rc = dev_alloc(ctx, &k.pos, n)) || (rc = dev_alloc(ctx, &k.vel, n)) || (rc = dev_alloc(ctx, &k.ids, n))))
+        return rc;
+    k.curPos = ctx->curPos; k.curVel = ctx->curVel; k.curPred = ctx->curPred; k.keysIdx = ctx->keysIdx;
+    PBF_CUDA(ctx, cudaMemcpyAsync(k.pos, ctx->pos[ctx->curPos], 16 * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaMemcpyAsync(k.vel, ctx->vel[ctx->curVel], 16 * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaMemcpyAsync(k.ids, ctx->ids, 4 * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    return PBF_OK;
+}
+
+int load_checkpoint(pbf_ctx* ctx, const pbf_ctx::Checkpoint& k) {
+    const size_t n = (size_t)ctx->n;
+    ctx->curPos = k.curPos; ctx->curVel = k.curVel; ctx->curPred = k.curPred; ctx->keysIdx = k.keysIdx;
+    PBF_CUDA(ctx, cudaMemcpyAsync(ctx->pos[ctx->curPos], k.pos, 16 * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaMemcpyAsync(ctx->vel[ctx->curVel], k.vel, 16 * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaMemcpyAsync(ctx->ids, k.ids, 4 * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    return PBF_OK;
+}
+
+void free_tape(pbf_ctx* ctx) {
+    for (void* p : ctx->tapeMem) cudaFree(p);
+    ctx->tapeMem.clear();
+    ctx->tapes.clear();
+    ctx->adj = pbf::AdjointBuffers{};
+    ctx->adjById = nullptr;
+    ctx->tapeEvery = ctx->tapeIters = 0;
+    ctx->tapeClamp = -1;
+}
+
+// One segment of tape (rollEvery substeps) and the adjoint buffers.
+int ensure_tape(pbf_ctx* ctx) {
+    const int n = ctx->n, iters = (int)ctx->params.simIterations, every = ctx->rollEvery;
+    const int clamp = ctx->params.boxClamp != 0;
+    if (ctx->tapeEvery == every && ctx->tapeIters == iters && ctx->tapeClamp == clamp) return PBF_OK;
+    free_tape(ctx);
+    const size_t v4 = 16 * (size_t)n;
+    bool ok = true;
+    auto take = [&](size_t bytes) -> void* {
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) { ok = false; return nullptr; }
+        ctx->tapeMem.push_back(p);
+        return p;
+    };
+    ctx->tapes.assign(every, pbf::AdjointTape{});
+    for (pbf::AdjointTape& t : ctx->tapes) {
+        t.iterations = iters;
+        t.perm = (uint32_t*)take(4 * (size_t)n);
+        t.list = (uint32_t*)take(4 * (size_t)ctx->listSlots * n);
+        t.meta = (uint2*)take(8 * (size_t)n);
+        for (int it = 0; it < iters; ++it) t.q[it] = (float4*)take(v4);
+        t.mask = clamp ? (uint8_t*)take((size_t)iters * n) : nullptr;
+        t.pI = (float4*)take(v4);
+        t.v2 = (float4*)take(v4);
+        t.omega = (float4*)take(v4);
+    }
+    pbf::AdjointBuffers& ab = ctx->adj;
+    float4** vecs[] = {&ab.xb, &ab.vb, &ab.xo, &ab.vo, &ab.pb, &ab.pbt, &ab.omb, &ab.v2b, &ab.xsb, &ctx->adjById};
+    for (float4** v : vecs) *v = (float4*)take(v4);
+    ab.lb = (float*)take(4 * (size_t)n);
+    ab.scalars = (float*)take(16);
+    cudaGetLastError();
+    if (!ok) {
+        free_tape(ctx);
+        return fail(ctx, PBF_ERR_CUDA, "pbf_rollout_backward: cannot allocate one segment of tape");
+    }
+    ctx->tapeEvery = every;
+    ctx->tapeIters = iters;
+    ctx->tapeClamp = clamp;
+    return PBF_OK;
+}
 }  // namespace
 
 // ================================================================ C-ABI ==
@@ -466,7 +570,10 @@ int pbf_destroy(pbf_ctx* ctx) {
     }
     dev_free(ctx->omega); dev_free(ctx->density); dev_free(ctx->hist); dev_free(ctx->cells);
     dev_free(ctx->list); dev_free(ctx->meta); dev_free(ctx->errWord);
-    dev_free(ctx->scenes); dev_free(ctx->sceneOf);
+    dev_free(ctx->scenes); dev_free(ctx->sceneOf); dev_free(ctx->ids); dev_free(ctx->idsTmp);
+    for (auto& k : ctx->ckpt) { dev_free(k.pos); dev_free(k.vel); dev_free(k.ids); }
+    dev_free(ctx->ckptEnd.pos); dev_free(ctx->ckptEnd.vel); dev_free(ctx->ckptEnd.ids);
+    free_tape(ctx);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PBF_OK;
@@ -491,7 +598,14 @@ int pbf_init_buffers(pbf_ctx* ctx, const float* init_pos, const float* init_vel)
         PBF_CUDA(ctx, cudaMemset(ctx->keys[k], 0, 4 * (size_t)n));
         PBF_CUDA(ctx, cudaMemset(ctx->pred[k], 0, 16 * (size_t)n));
     }
-    if ((rc = dev_alloc(ctx, &ctx->omega, n)) || (rc = dev_alloc(ctx, &ctx->density, n))) return rc;
+    if ((rc = dev_alloc(ctx, &ctx->omega, n)) || (rc = dev_alloc(ctx, &ctx->density, n)) ||
+        (rc = dev_alloc(ctx, &ctx->ids, n)) || (rc = dev_alloc(ctx, &ctx->idsTmp, n)))
+        return rc;
+    {
+        std::vector<uint32_t> iota(n);
+        for (int i = 0; i < n; ++i) iota[i] = (uint32_t)i;
+        PBF_CUDA(ctx, cudaMemcpy(ctx->ids, iota.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+    }
     PBF_CUDA(ctx, cudaMemset(ctx->omega, 0, 16 * (size_t)n));
     PBF_CUDA(ctx, cudaMemset(ctx->density, 0, 4 * (size_t)n));
     ctx->curPos = 0; ctx->curVel = 0; ctx->curPred = 1; ctx->keysIdx = 0; ctx->stepped = false;
@@ -668,7 +782,13 @@ int pbf_write_state(pbf_ctx* ctx, const float* pos, const float* vel) {
     if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers has not run");
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t bytes = 16 * (size_t)ctx->n;
-    if (pos) PBF_CUDA(ctx, cudaMemcpyAsync(ctx->pos[ctx->curPos], pos, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<uint32_t> iota;
+    if (pos) {
+        PBF_CUDA(ctx, cudaMemcpyAsync(ctx->pos[ctx->curPos], pos, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        iota.resize(ctx->n);  // the written records become particles 0 .. N-1
+        for (int i = 0; i < ctx->n; ++i) iota[i] = (uint32_t)i;
+        PBF_CUDA(ctx, cudaMemcpyAsync(ctx->ids, iota.data(), 4 * (size_t)ctx->n, cudaMemcpyHostToDevice, ctx->stream));
+    }
     if (vel) PBF_CUDA(ctx, cudaMemcpyAsync(ctx->vel[ctx->curVel], vel, bytes, cudaMemcpyHostToDevice, ctx->stream));
     PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return PBF_OK;
@@ -875,6 +995,79 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
     if (e != cudaSuccess) { ctx->shape = shape0; return fail(ctx, PBF_ERR_CUDA, std::string("pbf_autotune: ") + cudaGetErrorString(e)); }
     ctx->shape = pbf::LaunchShape{choice[0], choice[1], choice[2], choice[3], choice[4]};
     if (blocks_out) for (int q = 0; q < 5; ++q) blocks_out[q] = choice[q];
+    return read_error_word(ctx);
+}
+
+int pbf_read_ids(pbf_ctx* ctx, uint32_t* ids) {
+    if (!ctx || !ids) return fail(ctx, PBF_ERR_INVALID, "pbf_read_ids: NULL argument");
+    if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers has not run");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    PBF_CUDA(ctx, cudaMemcpyAsync(ids, ctx->ids, 4 * (size_t)ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PBF_OK;
+}
+
+int pbf_rollout_forward(pbf_ctx* ctx, int substeps, int checkpoint_every) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (is_batch(ctx)) return fail(ctx, PBF_ERR_UNSUPPORTED, "rollouts run on single-scene contexts");
+    if (ctx->paused) return fail(ctx, PBF_ERR_STATE, "rollouts need an unpaused simulation");
+    if (substeps < 1 || checkpoint_every < 1) return fail(ctx, PBF_ERR_INVALID, "substeps and checkpoint_every must be >= 1");
+    if (ctx->params.simIterations < 1 || ctx->params.simIterations > 64)
+        return fail(ctx, PBF_ERR_INVALID, "rollouts need 1..64 solver iterations");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int segments = (substeps + checkpoint_every - 1) / checkpoint_every;
+    for (auto& k : ctx->ckpt) { dev_free(k.pos); dev_free(k.vel); dev_free(k.ids); }
+    ctx->ckpt.assign(segments, pbf_ctx::Checkpoint{});
+    for (int sgm = 0; sgm < segments; ++sgm) {
+        if ((rc = save_checkpoint(ctx, ctx->ckpt[sgm]))) return rc;
+        const int len = std::min(checkpoint_every, substeps - sgm * checkpoint_every);
+        if ((rc = pbf_step_async(ctx, len))) return rc;
+    }
+    if ((rc = save_checkpoint(ctx, ctx->ckptEnd))) return rc;
+    ctx->rollSubsteps = substeps;
+    ctx->rollEvery = checkpoint_every;
+    return pbf_synchronize(ctx);
+}
+
+int pbf_rollout_backward(pbf_ctx* ctx, const float* dL_dx, float* dL_dv0, float* dL_dvisc, float* dL_dg) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!dL_dx) return fail(ctx, PBF_ERR_INVALID, "pbf_rollout_backward: dL_dx is NULL");
+    if (ctx->ckpt.empty() || ctx->rollSubsteps < 1) return fail(ctx, PBF_ERR_STATE, "pbf_rollout_forward has not run");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    if ((rc = ensure_tape(ctx))) return rc;
+    drop_graph(ctx);
+    const int n = ctx->n, iters = (int)ctx->params.simIterations, every = ctx->rollEvery;
+    const size_t v4 = 16 * (size_t)n;
+    cudaStream_t s = ctx->stream;
+    pbf::AdjointBuffers ab = ctx->adj;  // adjoint_substep swaps its pointers
+    PBF_CUDA(ctx, cudaMemcpyAsync(ctx->adjById, dL_dx, v4, cudaMemcpyHostToDevice, s));
+    pbf::scatter_by_id(n, ctx->ckptEnd.ids, ctx->adjById, ab.xb, s);
+    cudaMemsetAsync(ab.vb, 0, v4, s);
+    cudaMemsetAsync(ab.scalars, 0, 16, s);
+    ctx->launches += 1;
+    const int segments = (int)ctx->ckpt.size();
+    for (int sgm = segments - 1; sgm >= 0 && rc == PBF_OK; --sgm) {
+        if ((rc = load_checkpoint(ctx, ctx->ckpt[sgm]))) break;
+        const int len = std::min(every, ctx->rollSubsteps - sgm * every);
+        for (int k = 0; k < len && rc == PBF_OK; ++k) rc = enqueue_substep(ctx, nullptr, &ctx->tapes[k]);
+        for (int k = len - 1; k >= 0 && rc == PBF_OK; --k) {
+            pbf::adjoint_substep(ctx->consts, ctx->tapes[k], ab, s);
+            ctx->launches += pbf::adjoint_launches(iters);
+        }
+    }
+    if (rc) return rc;
+    pbf::gather_to_id(n, ctx->ckpt[0].ids, ab.vb, ctx->adjById, s);
+    ctx->launches += 1;
+    if (dL_dv0) PBF_CUDA(ctx, cudaMemcpyAsync(dL_dv0, ctx->adjById, v4, cudaMemcpyDeviceToHost, s));
+    float sc[4] = {0, 0, 0, 0};
+    PBF_CUDA(ctx, cudaMemcpyAsync(sc, ab.scalars, 16, cudaMemcpyDeviceToHost, s));
+    if ((rc = load_checkpoint(ctx, ctx->ckptEnd))) return rc;
+    PBF_CUDA(ctx, cudaStreamSynchronize(s));
+    PBF_CUDA(ctx, cudaGetLastError());
+    if (dL_dvisc) *dL_dvisc = sc[0];
+    if (dL_dg) { dL_dg[0] = sc[1]; dL_dg[1] = sc[2]; dL_dg[2] = sc[3]; }
     return read_error_word(ctx);
 }
 

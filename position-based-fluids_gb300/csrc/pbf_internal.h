@@ -64,8 +64,8 @@ void launch_predict_keys(const DevConsts& c, Batch b, const float4* pos, float4*
                          uint32_t* keys, uint32_t* perm, int paused, cudaStream_t s);
 void launch_compute_keys(const DevConsts& c, Batch b, const float4* pred, uint32_t* keys, uint32_t* perm,
                          cudaStream_t s);
-void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred,
-                          float4* posOut, float4* predOut, cudaStream_t s);
+void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, const uint32_t* ids,
+                          float4* posOut, float4* predOut, uint32_t* idsOut, cudaStream_t s);
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
 void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
@@ -74,9 +74,9 @@ void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* pred
                             const uint32_t* list, const uint2* meta, int block, cudaStream_t s);
 void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, float4* predOut,
                           const float* density, const uint32_t* list, const uint2* meta, int lastIteration,
-                          int block, cudaStream_t s);
+                          uint8_t* clampMask, int block, cudaStream_t s);
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
-                              float4* vel, cudaStream_t s);
+                              float4* vel, const uint32_t* idsIn, uint32_t* idsOut, cudaStream_t s);
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
                             float4* omega, const uint32_t* list, const uint2* meta, int block, cudaStream_t s);
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
@@ -99,5 +99,30 @@ int launch_radix_sort(const SortPlan& plan, uint32_t* keys[2], uint32_t* perm[2]
                       cudaStream_t s);
 // Kernels launched by one launch_radix_sort call.
 int radix_sort_launches(const SortPlan& plan);
+
+// ---- adjoint (pbf_adjoint.cu) ----
+// What one substep of a rollout leaves for its reverse pass.
+struct AdjointTape {
+    int iterations = 0;
+    uint32_t* perm = nullptr;      // sorted index k came from perm[k]
+    uint32_t* list = nullptr;      // friend rows of the substep
+    uint2* meta = nullptr;
+    float4* q[64] = {};            // (p^t, lambda^t), t < iterations
+    uint8_t* mask = nullptr;       // iterations x N box-clamp decisions (NULL: no clamp)
+    float4* pI = nullptr;          // final predictions, w = density
+    float4* v2 = nullptr;          // velocities before XSPH
+    float4* omega = nullptr;
+};
+// Adjoint state; xb / vb hold the adjoints of the substep's output on entry
+// and of its input on return (the pointers are swapped with xo / vo).
+struct AdjointBuffers {
+    float4 *xb, *vb, *xo, *vo, *pb, *pbt, *omb, *v2b, *xsb;
+    float* lb;
+    float* scalars;  // [0] dL/d viscosityFactor, [1..3] dL/d gravity
+};
+void adjoint_substep(const DevConsts& c, const AdjointTape& tp, AdjointBuffers& ab, cudaStream_t s);
+int adjoint_launches(int iterations);
+void scatter_by_id(int n, const uint32_t* ids, const float4* byId, float4* out, cudaStream_t s);
+void gather_to_id(int n, const uint32_t* ids, const float4* in, float4* byId, cudaStream_t s);
 
 }  // namespace pbf

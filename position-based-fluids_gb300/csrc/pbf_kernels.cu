@@ -27,12 +27,12 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+#include "pbf_device.cuh"
 #include "pbf_internal.h"
 
 namespace pbf {
 namespace {
 
-constexpr uint32_t kEmpty = 0xFFFFFFFFu;  // END_OF_CELL_LIST
 constexpr int kBlock = 256;
 
 inline unsigned blocks_for(int n, int block = kBlock) { return (unsigned)((n + block - 1) / block); }
@@ -41,26 +41,6 @@ inline unsigned blocks_for(int n, int block = kBlock) { return (unsigned)((n + b
 // single scene.
 __device__ __forceinline__ uint32_t key_base(const Batch& b, int i) {
     return b.scenes ? b.scenes[b.sceneOf[i]].keyBase : 0u;
-}
-
-// utilities.cl:69-77
-__device__ __forceinline__ uint32_t expand_bits(int xi) {
-    uint32_t x = (uint32_t)xi;
-    x = (x | (x << 16)) & 0x030000FFu;
-    x = (x | (x << 8)) & 0x0300F00Fu;
-    x = (x | (x << 4)) & 0x030C30C3u;
-    x = (x | (x << 2)) & 0x09249249u;
-    return x;
-}
-
-// utilities.cl:79-87 (the Morton number is non-negative, < 2^30).
-__device__ __forceinline__ uint32_t grid_hash(int x, int y, int z, uint32_t grid) {
-    uint32_t m = expand_bits(x) | (expand_bits(y) << 1) | (expand_bits(z) << 2);
-    return (grid & (grid - 1)) == 0 ? (m & (grid - 1)) : (m % grid);
-}
-
-__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
-    return (ax * bx + ay * by) + az * bz;
 }
 
 // ------------------------------------------------------------- predict --
@@ -105,14 +85,18 @@ __global__ void compute_keys_kernel(DevConsts c, Batch b, const float4* __restri
 
 // radixsort.cl:22-37 (velocities are not permuted; they are recomputed
 // before any read, update_velocities.cl:13).
+// Particle ids (the original index of each record) follow the same
+// permutation into idsOut.
 __global__ void gather_sorted_kernel(int n, const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
-                                     const float4* __restrict__ pred, float4* __restrict__ posOut,
-                                     float4* __restrict__ predOut) {
+                                     const float4* __restrict__ pred, const uint32_t* __restrict__ ids,
+                                     float4* __restrict__ posOut, float4* __restrict__ predOut,
+                                     uint32_t* __restrict__ idsOut) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t j = perm[i];
     posOut[i] = pos[j];
     predOut[i] = pred[j];
+    idsOut[i] = ids[j];
 }
 
 // --------------------------------------------------------------- cells --
@@ -138,16 +122,6 @@ __global__ void reset_cells_kernel(int n, const uint32_t* __restrict__ keys, uin
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     cells[keys[i]] = make_uint2(kEmpty, kEmpty);
-}
-
-// -------------------------------------------------------------- friends --
-__device__ __forceinline__ uint32_t byte_of(uint64_t v, int k) { return (uint32_t)(v >> (8 * k)) & 0xFFu; }
-__device__ __forceinline__ uint32_t circle_count(uint64_t meta, int k) { return (uint32_t)(meta >> (7 * k)) & 0x7Fu; }
-__device__ __forceinline__ int kept_density(uint64_t meta) { return (int)(meta >> 56) & 0xF; }
-__device__ __forceinline__ int kept_other(uint64_t meta) { return (int)(meta >> 60) & 0xF; }
-__device__ __forceinline__ uint64_t load_meta(const uint2* meta, int i) {
-    const uint2 m = meta[i];
-    return (uint64_t)m.x | ((uint64_t)m.y << 32);
 }
 
 // Number of leading circles a pass keeps: circles are visited in order and
@@ -226,60 +200,6 @@ build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, cons
     meta[i] = make_uint2((uint32_t)mt, (uint32_t)(mt >> 32));
 }
 
-// The friends of particle i that a pass keeps, as one flat sequence
-// t = 0 .. total-1 in circle-major order (the reference's summation order):
-// entry t of circle k sits in list row t + (k*perCircle - first(k)), where
-// first(k) is the number of entries of the circles before k.
-struct FriendRows {
-    uint64_t meta;
-    int perCircle, total, k, boundary, off;
-    __device__ __forceinline__ FriendRows(uint64_t m, int kept, int P) : meta(m), perCircle(P), k(0), off(0) {
-        total = 0;
-        for (int c = 0; c < kept; ++c) total += (int)circle_count(m, c);
-        boundary = (int)circle_count(m, 0);
-    }
-    // Rows are requested for t = 0, 1, 2, ... in order.
-    __device__ __forceinline__ int row(int t) {
-        while (t >= boundary) {
-            off += perCircle - (int)circle_count(meta, k);
-            ++k;
-            boundary += (int)circle_count(meta, k);
-        }
-        return t + off;
-    }
-};
-
-// Runs body(load(j)) for every kept friend j in order.  Neighbours are taken
-// U at a time: the U list entries are loaded, then the U neighbour records,
-// then the U bodies run in order, so the sums keep their sequential order
-// while U independent loads are in flight.
-template <int U, typename LoadF, typename BodyF>
-__device__ __forceinline__ void gather_friends(const uint32_t* __restrict__ list, int n, int i, FriendRows fr,
-                                               LoadF load, BodyF body) {
-    int t = 0;
-    for (; t + U <= fr.total; t += U) {
-        uint32_t j[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) j[u] = __ldg(list + (size_t)fr.row(t + u) * n + i);
-        decltype(load(0u)) rec[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) rec[u] = load(j[u]);
-#pragma unroll
-        for (int u = 0; u < U; ++u) body(rec[u]);
-    }
-    for (; t < fr.total; ++t) body(load(__ldg(list + (size_t)fr.row(t) * n + i)));
-}
-
-struct PairRec {
-    float4 a, b;
-};
-
-// A neighbour enters the solver sums when r^2 < h^2 and, with the
-// zero-distance guard, r^2 > 0.
-__device__ __forceinline__ bool in_support(const DevConsts& c, float r2) {
-    return r2 < c.h2 && (!c.guard || r2 > 0.0f);
-}
-
 // -------------------------------------------------------------- scaling --
 // compute_scaling.cl:27-112 followed by pack_data.cl (w = lambda).
 __global__ void __launch_bounds__(kMaxBlock)
@@ -326,7 +246,7 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
 __global__ void __launch_bounds__(kMaxBlock)
 compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, float4* __restrict__ predOut,
                      const float* __restrict__ density, const uint32_t* __restrict__ list,
-                     const uint2* __restrict__ meta, int lastIteration) {
+                     const uint2* __restrict__ meta, int lastIteration, uint8_t* __restrict__ clampMask) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
     if (i >= n) return;
@@ -363,9 +283,14 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, float4
             lo = sp.lo;
             hi = sp.hi;
         }
+        if (clampMask)  // which coordinates the clamp moves: 2 bits per axis, 1 low, 2 high
+            clampMask[i] = (uint8_t)((fx < lo[0] ? 1 : (fx > hi[0] ? 2 : 0)) | (fy < lo[1] ? 4 : (fy > hi[1] ? 8 : 0)) |
+                                     (fz < lo[2] ? 16 : (fz > hi[2] ? 32 : 0)));
         fx = fx < lo[0] ? lo[0] : (fx > hi[0] ? hi[0] : fx);
         fy = fy < lo[1] ? lo[1] : (fy > hi[1] ? hi[1] : fy);
         fz = fz < lo[2] ? lo[2] : (fz > hi[2] ? hi[2] : fz);
+    } else if (clampMask) {
+        clampMask[i] = 0;
     }
     const float dx = fx - pi.x, dy = fy - pi.y, dz = fz - pi.z;
     predOut[i] = make_float4(pi.x + dx, pi.y + dy, pi.z + dz, lastIteration ? density[i] : pi.w + 0.0f);
@@ -373,11 +298,14 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, float4
 
 // ----------------------------------------------------------- velocities --
 // update_velocities.cl:11-14 (the GL texture write is dropped).
+// Also moves the sorted particle ids back to their fixed buffer.
 __global__ void update_velocities_kernel(DevConsts c, const float4* __restrict__ pred,
                                          const float4* __restrict__ posIn, float4* __restrict__ posOut,
-                                         float4* __restrict__ vel) {
+                                         float4* __restrict__ vel, const uint32_t* __restrict__ idsIn,
+                                         uint32_t* __restrict__ idsOut) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
+    if (idsIn) idsOut[i] = idsIn[i];
     const float4 p = pred[i], q = posIn[i];
     float4 v = vel[i];
     v.x = (p.x - q.x) / c.dt;
@@ -487,9 +415,9 @@ void launch_compute_keys(const DevConsts& c, Batch b, const float4* pred, uint32
     compute_keys_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, b, pred, keys, perm);
 }
 
-void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, float4* posOut,
-                          float4* predOut, cudaStream_t s) {
-    gather_sorted_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, perm, pos, pred, posOut, predOut);
+void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, const uint32_t* ids,
+                          float4* posOut, float4* predOut, uint32_t* idsOut, cudaStream_t s) {
+    gather_sorted_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, perm, pos, pred, ids, posOut, predOut, idsOut);
 }
 
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s) {
@@ -513,14 +441,14 @@ void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* pred
 
 void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, float4* predOut,
                           const float* density, const uint32_t* list, const uint2* meta, int lastIteration,
-                          int block, cudaStream_t s) {
+                          uint8_t* clampMask, int block, cudaStream_t s) {
     compute_delta_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, b, predPacked, predOut, density, list, meta,
-                                                                  lastIteration);
+                                                                  lastIteration, clampMask);
 }
 
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
-                              float4* vel, cudaStream_t s) {
-    update_velocities_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, posIn, posOut, vel);
+                              float4* vel, const uint32_t* idsIn, uint32_t* idsOut, cudaStream_t s) {
+    update_velocities_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c, pred, posIn, posOut, vel, idsIn, idsOut);
 }
 
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,

@@ -111,6 +111,9 @@ def library() -> ctypes.CDLL:
         "pbf_get_launch_shape": [c_void_p, POINTER(c_int)],
         "pbf_set_launch_shape": [c_void_p, POINTER(c_int)],
         "pbf_autotune": [c_void_p, c_int, POINTER(c_int)],
+        "pbf_read_ids": [c_void_p, u32p],
+        "pbf_rollout_forward": [c_void_p, c_int, c_int],
+        "pbf_rollout_backward": [c_void_p, f32p, f32p, POINTER(c_float), f32p],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -345,6 +348,29 @@ class Simulation:
     def use_graph(self, on: bool) -> None:
         _check(self.lib.pbf_use_graph(self._ctx, int(on)), self._ctx)
 
+    def read_ids(self) -> np.ndarray:
+        ids = np.empty(self.n, np.uint32)
+        _check(self.lib.pbf_read_ids(self._ctx, _u32(ids)), self._ctx)
+        return ids
+
+    def positions_by_id(self) -> np.ndarray:
+        pos, _, _ = self.read_state()
+        out = np.empty_like(pos)
+        out[self.read_ids()] = pos
+        return out
+
+    def rollout_forward(self, substeps: int, checkpoint_every: int = 10) -> None:
+        _check(self.lib.pbf_rollout_forward(self._ctx, substeps, checkpoint_every), self._ctx)
+
+    def rollout_backward(self, dL_dx_by_id: np.ndarray):
+        """(dL/dv0 [N,4] by original index, dL/d viscosityFactor, dL/d gravity [3])."""
+        gx = np.ascontiguousarray(dL_dx_by_id, np.float32).reshape(self.n, 4)
+        dv = np.zeros((self.n, 4), np.float32)
+        dc = c_float(0)
+        dg = np.zeros(3, np.float32)
+        _check(self.lib.pbf_rollout_backward(self._ctx, _f32(gx), _f32(dv), ctypes.byref(dc), _f32(dg)), self._ctx)
+        return dv, dc.value, dg
+
     def scene_offsets(self) -> np.ndarray:
         k = len(self.scene_params) if self.scene_params else 1
         out = np.zeros(k + 1, np.uint32)
@@ -375,6 +401,7 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_enable_stage_timing", "pbf_stage_timings", "pbf_launch_count", "pbf_use_graph",
         "pbf_reference_lattice", "pbf_scene_block", "pbf_sort_state_noalloc", "pbf_scene_double_dam_break",
         "pbf_create_batch", "pbf_scene_offsets", "pbf_get_launch_shape", "pbf_set_launch_shape", "pbf_autotune",
+        "pbf_read_ids", "pbf_rollout_forward", "pbf_rollout_backward",
     ])
 
 
@@ -419,6 +446,38 @@ def make_double_dam_break(n: int, iterations: int = 4, seed: int = 20240601, fil
     params.xMin, params.xMax, params.yMin, params.yMax, params.zMin, params.zMax = (float(b) for b in box)
     params.gridBufSize = grid_size_for_box(box, params.h)
     return params, pos, np.zeros_like(pos)
+
+
+def make_rollout_scene(nx: int = 64, ny: int = 32, nz: int = 32, seed: int = 20240601):
+    """(params, pos, vel) of the differentiable-rollout dam break: an
+    nx x ny x nz block (spacing 0.05, jitter 0.005, origin 0.025) in the low
+    corner of a (2 nx, ny, nz) x 0.05 box, the dam_break_32k solver settings,
+    gravity as the vector (0, -9.8, 0) so that it can be differentiated."""
+    params = load_scenario("dam_break_32k")
+    s = 0.05
+    pos = scene_block(nx, ny, nz, s, (0.025, 0.025, 0.025), 0.005, seed)
+    params.particleCount = nx * ny * nz
+    box = (0.0, 2 * nx * s, 0.0, ny * s, 0.0, nz * s)
+    params.xMin, params.xMax, params.yMin, params.yMax, params.zMin, params.zMax = box
+    params.gridBufSize = grid_size_for_box(box, params.h)
+    params.gravityVectorEnable = 1
+    params.gravityX, params.gravityY, params.gravityZ = 0.0, -float(params.garvity), 0.0
+    return params, pos, np.zeros_like(pos)
+
+
+def rollout_target_params(params: PbfParameters, tilt_degrees: float = 5.0, xsph_c: float = 0.03) -> PbfParameters:
+    """Parameters of the rollout's target run: gravity tilted by
+    `tilt_degrees` towards +x and the XSPH factor c (in the units of the
+    reference's ViscosityFactor times the rest density, as in the batched
+    scenes: viscosityFactor = c / restDensity)."""
+    import math
+    p = PbfParameters.from_buffer_copy(params)
+    g = float(params.garvity)
+    t = math.radians(tilt_degrees)
+    p.gravityVectorEnable = 1
+    p.gravityX, p.gravityY, p.gravityZ = g * math.sin(t), -g * math.cos(t), 0.0
+    p.viscosityFactor = xsph_c / float(params.restDensity)
+    return p
 
 
 def make_batch_scenes(count: int = 256, seed: int = 7, fill: float = 0.3, first: int | None = None):
