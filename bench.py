@@ -202,6 +202,7 @@ def gpu_arm(args) -> None:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     params, pos, vel = pbf.make_scene(args.scene)
+    params.relaxedMath = 1 if args.math == "relaxed" else 0
     n, iters, sub = int(params.particleCount), int(params.simIterations), int(params.subSteps)
     sim = pbf.Simulation.create(params, pos, vel, device=local)
     stream = torch.cuda.ExternalStream(sim.stream(), device=torch.device("cuda", local))
@@ -280,6 +281,24 @@ def gpu_arm(args) -> None:
     if dominant == TRAFFIC_CAPTURE["kernel"]:
         scale = STAGE_BYTES[dominant](nl, nd) / STAGE_BYTES[dominant](TRAFFIC_CAPTURE["nl"], TRAFFIC_CAPTURE["nl"])
         traffic = TRAFFIC_CAPTURE["bytes"] * scale
+    # ---- the other arithmetic mode, same scene state and block sizes ----
+    other = "exact" if args.math == "relaxed" else "relaxed"
+    p2 = params.copy()
+    p2.relaxedMath = 1 if other == "relaxed" else 0
+    sim.set_params(p2)
+    for _ in range(3):
+        sim.step_async(sub)
+    barrier()
+    o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    o0.record(stream)
+    for _ in range(args.steps):
+        sim.step_async(sub)
+    o1.record(stream)
+    o1.synchronize()
+    other_ms = o0.elapsed_time(o1) / args.steps
+    other_line = {"mode": other, "value": n * iters * sub / (other_ms / 1000.0), "ms_per_step": other_ms}
+    sim.set_params(params)
+
     frame_ms = ms / args.steps
     bytes_sub = (444.0 + 56.0 * iters) * n  # whole-substep compulsory bytes, P = 3 sort passes
     pipeline_gbs = bytes_sub * sub / (frame_ms / 1000.0) / 1e9
@@ -300,7 +319,7 @@ def gpu_arm(args) -> None:
                                f"in a 12.8x6.4x6.4 box; {iters} iterations x {sub} substeps per step (frame)",
                    "particles": n, "iterations": iters, "substeps_per_step": sub,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "working set larger than L2 (no flush)", "mode": "reference-exact FP32 (no FMA contraction)",
+                   "l2": "working set larger than L2 (no flush)", "mode": MODES[args.math],
                    "cuda_graph": True,
                    "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity"], blocks))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
@@ -313,6 +332,7 @@ def gpu_arm(args) -> None:
                               "frac": pipeline_gbs / peak},
         "stage_ms_per_step": {k: round(v, 4) for k, v in sorted(stage_ms.items(), key=lambda kv: -kv[1])},
         "neighbours": {"density_pass": nl, "other_passes": nd},
+        "other_mode": other_line,
         "clocks": clocks.summary(),
     }
     if base is not None:
@@ -321,6 +341,14 @@ def gpu_arm(args) -> None:
     sim.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+MODES = {
+    "relaxed": "relaxedMath 1: the four neighbour passes in relaxed FP32 (one rsqrt per pair, FMA), as the "
+               "reference's -cl-fast-relaxed-math build; one substep of positions within 1e-5 relative of the "
+               "exact oracle, velocities within exact FP32's own error against FP64",
+    "exact": "relaxedMath 0: strict IEEE FP32 in the reference's operation order, bit-identical to the oracle",
+}
 
 
 # Stage groups of the particle-count sweep.
@@ -533,6 +561,8 @@ def main() -> None:
     ap.add_argument("--cpu-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default block sizes")
+    ap.add_argument("--math", choices=["relaxed", "exact"], default="exact",
+                    help="relaxedMath of the timed scene (the other mode is timed beside it)")
     ap.add_argument("--sweep", action="store_true", help="particle-count sweep (double dam break) instead")
     ap.add_argument("--sweep-counts", default="262144,2097152,8388608")
     ap.add_argument("--sweep-steps", type=int, default=20)

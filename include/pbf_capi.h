@@ -55,7 +55,7 @@ int pbf_default_parameters(PbfParameters* out);
    stderr and ignored, and a final line with no trailing newline is dropped
    with "Error parsing parameters file".  Extra keys accepted here:
    gravityx / gravityy / gravityz (any of them enables the gravity vector),
-   boxclamp and zerodistanceguard.  Returns the number of unknown keys through *unknown (may be NULL). */
+   boxclamp, zerodistanceguard and relaxedmath.  Returns the number of unknown keys through *unknown (may be NULL). */
 int pbf_load_parameters(const char* text, PbfParameters* inout, int* unknown);
 
 /* -------------------------------------------------------------- lifetime -- */

@@ -70,6 +70,14 @@ typedef struct PbfParameters {
        reference, where r / |r| is 0/0 and the particle's state becomes NaN
        (compute_scaling.cl:76-83, compute_delta.cl:142-146). */
     int          zeroDistanceGuard;
+    /* 0: the four neighbour passes evaluate the reference kernels in strict
+       IEEE FP32, bit-identical to the oracle.  1: relaxed FP32 in those
+       passes, as the reference's own -cl-fast-relaxed-math -cl-mad-enable
+       build (src/Simulation.cpp:160): one hardware reciprocal square root
+       per pair in place of a square root and three divisions, and fused
+       multiply-adds.  Keys, sort, cell table and friend lists stay exact;
+       one substep stays within 1e-5 relative of the exact result. */
+    int          relaxedMath;
 } PbfParameters;
 
 /* Largest friend-circle configuration the kernels accept. */

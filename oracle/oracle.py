@@ -50,6 +50,8 @@ def lib() -> ctypes.CDLL:
         l.oracle_rollout_grad_f64.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                               c_void_p]
         l.oracle_rollout_grad_f64.restype = c_double
+        l.oracle_rollout_grad_f32.argtypes = [c_void_p] * 8
+        l.oracle_rollout_grad_f32.restype = c_double
         _lib = l
     return _lib
 
@@ -223,4 +225,18 @@ class Rollout:
         dg = np.zeros(3, np.float64)
         loss = lib().oracle_rollout_grad_f64(self.handle, _ptr(g), None if vc is None else ctypes.byref(vc), _ptr(p0),
                                              _ptr(v0), _ptr(tgt), _ptr(dv), ctypes.byref(dc), _ptr(dg))
+        return loss, dv, dc.value, dg
+
+    def grad_f32(self, target, dl_dx=None):
+        """The same reverse pass evaluated in FP32 (serial, fixed order):
+        (loss, dL/dv0 [n,4], dL/dc, dL/dg [3]) as float64 arrays."""
+        p0 = np.ascontiguousarray(self.pos0, np.float64)
+        v0 = np.ascontiguousarray(self.vel0, np.float64)
+        tgt = np.ascontiguousarray(target, np.float64)
+        dx = None if dl_dx is None else np.ascontiguousarray(dl_dx, np.float64)
+        dv = np.zeros((self.n, 4), np.float64)
+        dc = c_double(0)
+        dg = np.zeros(3, np.float64)
+        loss = lib().oracle_rollout_grad_f32(self.handle, _ptr(p0), _ptr(v0), _ptr(tgt), _ptr(dx), _ptr(dv),
+                                             ctypes.byref(dc), _ptr(dg))
         return loss, dv, dc.value, dg

@@ -1074,22 +1074,27 @@ void oracle_rollout_free(void* handle) { delete static_cast<RolloutRecord*>(hand
 // viscosityFactor *visc (NULL: the recorded values).  Writes the final positions by original
 // index to pos_by_id (4n, may be NULL) and returns the loss
 // mean_{i,axis} (x_final - target)^2 against target_by_id (4n, may be NULL).
-static Consts<double> replay_consts(const RolloutRecord& rec, const double* g, const double* visc) {
-    Consts<double> c = make_consts<double>(rec.params);
-    if (g) { c.gx = g[0]; c.gy = g[1]; c.gz = g[2]; }
-    if (visc) c.visc = *visc;
+extern "C++" {
+template <typename T>
+static Consts<T> replay_consts(const RolloutRecord& rec, const double* g, const double* visc) {
+    Consts<T> c = make_consts<T>(rec.params);
+    if (g) { c.gx = (T)g[0]; c.gy = (T)g[1]; c.gz = (T)g[2]; }
+    if (visc) c.visc = (T)*visc;
     return c;
 }
 
+template <typename T>
 static double replay(const RolloutRecord& rec, const double* g, const double* visc, const double* pos0,
                      const double* vel0, const double* target_by_id, double* pos_by_id,
-                     std::vector<Tape<double>>* tapes, std::vector<V4<double>>* xFinal,
+                     std::vector<Tape<T>>* tapes, std::vector<V4<T>>* xFinal,
                      std::vector<uint32_t>* idsFinal) {
-    Consts<double> c = replay_consts(rec, g, visc);
+    Consts<T> c = replay_consts<T>(rec, g, visc);
     const int n = rec.n;
-    std::vector<V4<double>> x(n), v(n);
-    std::memcpy(x.data(), pos0, 32 * (size_t)n);
-    std::memcpy(v.data(), vel0, 32 * (size_t)n);
+    std::vector<V4<T>> x(n), v(n);
+    for (int i = 0; i < n; ++i) {
+        x[i] = {(T)pos0[4 * i], (T)pos0[4 * i + 1], (T)pos0[4 * i + 2], (T)pos0[4 * i + 3]};
+        v[i] = {(T)vel0[4 * i], (T)vel0[4 * i + 1], (T)vel0[4 * i + 2], (T)vel0[4 * i + 3]};
+    }
     std::vector<uint32_t> ids(n);
     for (int i = 0; i < n; ++i) ids[i] = (uint32_t)i;
     if (tapes) tapes->assign(rec.steps.size(), {});
@@ -1098,10 +1103,11 @@ static double replay(const RolloutRecord& rec, const double* g, const double* vi
     double loss = 0;
     for (int k = 0; k < n; ++k) {
         const uint32_t id = ids[k];
-        if (pos_by_id) { pos_by_id[4 * id] = x[k].x; pos_by_id[4 * id + 1] = x[k].y; pos_by_id[4 * id + 2] = x[k].z; pos_by_id[4 * id + 3] = 0; }
+        const double px = x[k].x, py = x[k].y, pz = x[k].z;
+        if (pos_by_id) { pos_by_id[4 * id] = px; pos_by_id[4 * id + 1] = py; pos_by_id[4 * id + 2] = pz; pos_by_id[4 * id + 3] = 0; }
         if (target_by_id) {
-            const double* t = target_by_id + 4 * (size_t)id;
-            loss += (x[k].x - t[0]) * (x[k].x - t[0]) + (x[k].y - t[1]) * (x[k].y - t[1]) + (x[k].z - t[2]) * (x[k].z - t[2]);
+            const double* tg = target_by_id + 4 * (size_t)id;
+            loss += (px - tg[0]) * (px - tg[0]) + (py - tg[1]) * (py - tg[1]) + (pz - tg[2]) * (pz - tg[2]);
         }
     }
     if (xFinal) *xFinal = x;
@@ -1109,10 +1115,48 @@ static double replay(const RolloutRecord& rec, const double* g, const double* vi
     return loss / (3.0 * n);
 }
 
+// Reverse pass in T after a replay in T; dL/dx from the replay's own final
+// positions, or from dl_dx_by_id (4n doubles, original order) when given.
+template <typename T>
+static double grad(const RolloutRecord& rec, const double* g, const double* visc, const double* pos0,
+                   const double* vel0, const double* target_by_id, const double* dl_dx_by_id, double* dv0,
+                   double* dvisc, double* dg) {
+    std::vector<Tape<T>> tapes;
+    std::vector<V4<T>> x;
+    std::vector<uint32_t> ids;
+    const double loss = replay<T>(rec, g, visc, pos0, vel0, target_by_id, nullptr, &tapes, &x, &ids);
+    Consts<T> c = replay_consts<T>(rec, g, visc);
+    const int n = rec.n;
+    std::vector<V4<T>> xb(n), vb(n, V4<T>{0, 0, 0, 0});
+    for (int k = 0; k < n; ++k) {
+        if (dl_dx_by_id) {
+            const double* d = dl_dx_by_id + 4 * (size_t)ids[k];
+            xb[k] = {(T)d[0], (T)d[1], (T)d[2], 0};
+        } else {
+            const double* tg = target_by_id + 4 * (size_t)ids[k];
+            const double s = 2.0 / (3.0 * n);
+            xb[k] = {(T)(s * ((double)x[k].x - tg[0])), (T)(s * ((double)x[k].y - tg[1])),
+                     (T)(s * ((double)x[k].z - tg[2])), 0};
+        }
+    }
+    T cb = 0, gb[3] = {0, 0, 0};
+    for (size_t k = rec.steps.size(); k-- > 0;)
+        adjoint_substep(rec.steps[k], c, (int)rec.params.simIterations, tapes[k], xb, vb, cb, gb);
+    if (dv0)
+        for (int i = 0; i < n; ++i) {
+            dv0[4 * i] = vb[i].x; dv0[4 * i + 1] = vb[i].y; dv0[4 * i + 2] = vb[i].z; dv0[4 * i + 3] = vb[i].w;
+        }
+    if (dvisc) *dvisc = cb;
+    if (dg) for (int k = 0; k < 3; ++k) dg[k] = gb[k];
+    return loss;
+}
+
+}  // extern "C++"
+
 double oracle_rollout_replay_f64(void* handle, const double* g, const double* visc, const double* pos0,
                                  const double* vel0, const double* target_by_id, double* pos_by_id) {
-    return replay(*static_cast<RolloutRecord*>(handle), g, visc, pos0, vel0, target_by_id, pos_by_id, nullptr, nullptr,
-                  nullptr);
+    return replay<double>(*static_cast<RolloutRecord*>(handle), g, visc, pos0, vel0, target_by_id, pos_by_id, nullptr,
+                          nullptr, nullptr);
 }
 
 // Loss and its exact gradient (FP64) with respect to the initial velocities
@@ -1121,26 +1165,17 @@ double oracle_rollout_replay_f64(void* handle, const double* g, const double* vi
 // recorded).
 double oracle_rollout_grad_f64(void* handle, const double* g, const double* visc, const double* pos0,
                                const double* vel0, const double* target_by_id, double* dv0, double* dvisc, double* dg) {
-    const RolloutRecord& rec = *static_cast<RolloutRecord*>(handle);
-    std::vector<Tape<double>> tapes;
-    std::vector<V4<double>> x;
-    std::vector<uint32_t> ids;
-    const double loss = replay(rec, g, visc, pos0, vel0, target_by_id, nullptr, &tapes, &x, &ids);
-    Consts<double> c = replay_consts(rec, g, visc);
-    const int n = rec.n;
-    std::vector<V4<double>> xb(n), vb(n, V4<double>{0, 0, 0, 0});
-    for (int k = 0; k < n; ++k) {
-        const double* t = target_by_id + 4 * (size_t)ids[k];
-        const double s = 2.0 / (3.0 * n);
-        xb[k] = {s * (x[k].x - t[0]), s * (x[k].y - t[1]), s * (x[k].z - t[2]), 0};
-    }
-    double cb = 0, gb[3] = {0, 0, 0};
-    for (size_t k = rec.steps.size(); k-- > 0;)
-        adjoint_substep(rec.steps[k], c, (int)rec.params.simIterations, tapes[k], xb, vb, cb, gb);
-    if (dv0) std::memcpy(dv0, vb.data(), 32 * (size_t)n);
-    if (dvisc) *dvisc = cb;
-    if (dg) for (int k = 0; k < 3; ++k) dg[k] = gb[k];
-    return loss;
+    return grad<double>(*static_cast<RolloutRecord*>(handle), g, visc, pos0, vel0, target_by_id, nullptr, dv0, dvisc,
+                        dg);
+}
+
+// The same replay and reverse pass evaluated in FP32, serially: the size of
+// the gradient error that FP32 arithmetic alone gives, in a fixed summation
+// order.  dl_dx_by_id may be NULL (dL/dx from the FP32 replay and target).
+double oracle_rollout_grad_f32(void* handle, const double* pos0, const double* vel0, const double* target_by_id,
+                               const double* dl_dx_by_id, double* dv0, double* dvisc, double* dg) {
+    return grad<float>(*static_cast<RolloutRecord*>(handle), nullptr, nullptr, pos0, vel0, target_by_id, dl_dx_by_id,
+                       dv0, dvisc, dg);
 }
 
 // Morton hash of one cell (utilities.cl:84-87).

@@ -87,6 +87,7 @@ extern "C" int pbf_load_parameters(const char* text, PbfParameters* p, int* unkn
         else if (key == "gravityz") { fields >> p->gravityZ; p->gravityVectorEnable = 1; }
         else if (key == "boxclamp") fields >> p->boxClamp;
         else if (key == "zerodistanceguard") fields >> p->zeroDistanceGuard;
+        else if (key == "relaxedmath") fields >> p->relaxedMath;
         else {
             std::cerr << "Unknown parameter " << key << std::endl << "Leaving it out." << std::endl;
             ++nUnknown;

@@ -180,6 +180,9 @@ DevConsts make_consts(const PbfParameters& p, int n) {
     c.hi[0] = p.xMax; c.hi[1] = p.yMax; c.hi[2] = p.zMax;
     c.clamp = p.boxClamp ? 1 : 0;
     c.guard = p.zeroDistanceGuard ? 1 : 0;
+    c.relaxed = p.relaxedMath ? 1 : 0;
+    c.dpScale = c.negGradSpiky / c.rho0;
+    c.invPoly6q = 1.0f / c.poly6q;
     c.circles = (int)p.friendsCircles;
     c.perCircle = (int)p.particlesPerCircle;
     c.grid = p.gridBufSize;
@@ -259,7 +262,8 @@ int check_batch_compatible(pbf_ctx* ctx, const std::vector<PbfParameters>& sp) {
                           a.vorticityFactor == b.vorticityFactor && a.surfaceTenstionK == b.surfaceTenstionK &&
                           a.surfaceTenstionDist == b.surfaceTenstionDist && a.friendsCircles == b.friendsCircles &&
                           a.particlesPerCircle == b.particlesPerCircle && a.gridBufSize == b.gridBufSize &&
-                          a.boxClamp == b.boxClamp && a.zeroDistanceGuard == b.zeroDistanceGuard;
+                          a.boxClamp == b.boxClamp && a.zeroDistanceGuard == b.zeroDistanceGuard &&
+                          a.relaxedMath == b.relaxedMath;
         if (!same)
             return fail(ctx, PBF_ERR_INVALID,
                         "scene " + std::to_string(s) + " differs from scene 0 in a parameter scenes must share "

@@ -20,6 +20,8 @@ struct DevConsts {
     float gx, gy, gz;
     float lo[3], hi[3];
     int clamp, guard;
+    int relaxed;                 // relaxedMath: the neighbour passes' relaxed variants
+    float dpScale, invPoly6q;    // -gradSpiky / rho0 and 1 / poly6q (relaxed variants only)
     int circles, perCircle;
     uint32_t grid;
     int n;

@@ -201,7 +201,19 @@ build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, cons
 }
 
 // -------------------------------------------------------------- scaling --
+// Relaxed variants (R = true, relaxedMath): per pair one reciprocal square
+// root w = 1/|r| replaces sqrt(r^2) and the divisions by |r|, and sums are
+// fused multiply-adds: the reference's kernels as its own
+// -cl-fast-relaxed-math -cl-mad-enable build may evaluate them.
+// Spiky gradient magnitude over |r|: (h - |r|)^2 / |r| with |r| = r^2 w.
+__device__ __forceinline__ float spiky_over_r(const DevConsts& c, float r2, float& w) {
+    w = rsqrtf(r2);
+    const float hr = fmaf(-r2, w, c.h);
+    return hr * hr * w;
+}
+
 // compute_scaling.cl:27-112 followed by pack_data.cl (w = lambda).
+template <bool R>
 __global__ void __launch_bounds__(kMaxBlock)
 compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __restrict__ predPacked,
                        float* __restrict__ density, const uint32_t* __restrict__ list,
@@ -216,18 +228,33 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
     gather_friends<U>(list, n, i, FriendRows(mt, kept_density(mt), c.perCircle),
                       [&](uint32_t j) { return __ldg(pred + j); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-        if (in_support(c, r2)) {
-            const float rl = sqrtf(r2);
-            const float hr = c.h - rl;
-            const float sc = c.gradSpiky * hr * hr;
-            const float g0 = (sc * rx) / rl, g1 = (sc * ry) / rl, g2 = (sc * rz) / rl;
-            const float d = c.h2 - r2;
-            ds = ds + d * d * d;
-            gsk = gsk + dot3(g0, g1, g2, g0, g1, g2);
-            gx = gx + g0;
-            gy = gy + g1;
-            gz = gz + g2;
+        if (R) {
+            const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
+            if (in_support(c, r2)) {
+                float w;
+                const float s = c.gradSpiky * spiky_over_r(c, r2, w);
+                const float g0 = s * rx, g1 = s * ry, g2 = s * rz;
+                const float d = c.h2 - r2;
+                ds = fmaf(d * d, d, ds);
+                gsk = fmaf(g2, g2, fmaf(g1, g1, fmaf(g0, g0, gsk)));
+                gx += g0;
+                gy += g1;
+                gz += g2;
+            }
+        } else {
+            const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+            if (in_support(c, r2)) {
+                const float rl = sqrtf(r2);
+                const float hr = c.h - rl;
+                const float sc = c.gradSpiky * hr * hr;
+                const float g0 = (sc * rx) / rl, g1 = (sc * ry) / rl, g2 = (sc * rz) / rl;
+                const float d = c.h2 - r2;
+                ds = ds + d * d * d;
+                gsk = gsk + dot3(g0, g1, g2, g0, g1, g2);
+                gx = gx + g0;
+                gy = gy + g1;
+                gz = gz + g2;
+            }
         }
     });
     ds = ds * c.poly6;
@@ -243,6 +270,7 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
 // the optional box clamp on `future`, then update_predicted.cl.  After the
 // last iteration w carries the density (pack_data.cl with the density source,
 // src/Simulation.cpp:591).
+template <bool R>
 __global__ void __launch_bounds__(kMaxBlock)
 compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, float4* __restrict__ predOut,
                      const float* __restrict__ density, const uint32_t* __restrict__ list,
@@ -257,24 +285,46 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, float4
     gather_friends<U>(list, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
                       [&](uint32_t j) { return __ldg(pp + j); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-        if (in_support(c, r2)) {
-            const float rl = sqrtf(r2);
-            const float hr = c.h - rl;
-            const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
-            const float d = c.h2 - r2;
-            const float p6 = d * d * d;
-            const float rq = p6 / c.poly6q;
-            const float scorr = c.K * rq * rq * rq * rq;
-            const float a = pi.w + pj.w + scorr;
-            sx = sx + a * g0;
-            sy = sy + a * g1;
-            sz = sz + a * g2;
+        if (R) {
+            const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
+            if (in_support(c, r2)) {
+                float w;
+                const float k = spiky_over_r(c, r2, w);
+                const float d = c.h2 - r2;
+                const float rq = d * d * d * c.invPoly6q;
+                const float rq2 = rq * rq;
+                const float a = fmaf(c.K * rq2, rq2, pi.w + pj.w) * k;
+                sx = fmaf(a, rx, sx);
+                sy = fmaf(a, ry, sy);
+                sz = fmaf(a, rz, sz);
+            }
+        } else {
+            const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+            if (in_support(c, r2)) {
+                const float rl = sqrtf(r2);
+                const float hr = c.h - rl;
+                const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
+                const float d = c.h2 - r2;
+                const float p6 = d * d * d;
+                const float rq = p6 / c.poly6q;
+                const float scorr = c.K * rq * rq * rq * rq;
+                const float a = pi.w + pj.w + scorr;
+                sx = sx + a * g0;
+                sy = sy + a * g1;
+                sz = sz + a * g2;
+            }
         }
     });
-    float fx = pi.x + (c.negGradSpiky * sx) / c.rho0;
-    float fy = pi.y + (c.negGradSpiky * sy) / c.rho0;
-    float fz = pi.z + (c.negGradSpiky * sz) / c.rho0;
+    float fx, fy, fz;
+    if (R) {
+        fx = fmaf(c.dpScale, sx, pi.x);
+        fy = fmaf(c.dpScale, sy, pi.y);
+        fz = fmaf(c.dpScale, sz, pi.z);
+    } else {
+        fx = pi.x + (c.negGradSpiky * sx) / c.rho0;
+        fy = pi.y + (c.negGradSpiky * sy) / c.rho0;
+        fz = pi.z + (c.negGradSpiky * sz) / c.rho0;
+    }
     if (c.clamp) {
         const float* lo = c.lo;
         const float* hi = c.hi;
@@ -317,6 +367,7 @@ __global__ void update_velocities_kernel(DevConsts c, const float4* __restrict__
 
 // apply_viscosity.cl:12-86, every neighbour read from the pre-pass
 // velocities (Jacobi).
+template <bool R>
 __global__ void __launch_bounds__(kMaxBlock)
 apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const float4* __restrict__ velIn,
                        float4* __restrict__ velOut, float4* __restrict__ omega,
@@ -337,16 +388,29 @@ apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, co
             const float4 vj = q.b;
             const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
             const float d = c.h2 - r2;
-            const float rl = sqrtf(r2);
-            const float hr = c.h - rl;
-            const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
-            ox = ox + (uy * g2 - uz * g1);
-            oy = oy + (uz * g0 - ux * g2);
-            oz = oz + (ux * g1 - uy * g0);
-            const float d3 = d * d * d;
-            vsx = vsx + ux * d3;
-            vsy = vsy + uy * d3;
-            vsz = vsz + uz * d3;
+            if (R) {
+                float w;
+                const float k = spiky_over_r(c, r2, w);
+                const float g0 = k * rx, g1 = k * ry, g2 = k * rz;
+                ox += fmaf(uy, g2, -uz * g1);
+                oy += fmaf(uz, g0, -ux * g2);
+                oz += fmaf(ux, g1, -uy * g0);
+                const float d3 = d * d * d;
+                vsx = fmaf(ux, d3, vsx);
+                vsy = fmaf(uy, d3, vsy);
+                vsz = fmaf(uz, d3, vsz);
+            } else {
+                const float rl = sqrtf(r2);
+                const float hr = c.h - rl;
+                const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
+                ox = ox + (uy * g2 - uz * g1);
+                oy = oy + (uz * g0 - ux * g2);
+                oz = oz + (ux * g1 - uy * g0);
+                const float d3 = d * d * d;
+                vsx = vsx + ux * d3;
+                vsy = vsy + uy * d3;
+                vsz = vsz + uz * d3;
+            }
         }
     });
     vsx = vsx * c.poly6;
@@ -358,6 +422,7 @@ apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, co
 }
 
 // apply_vorticity.cl:12-86
+template <bool R>
 __global__ void __launch_bounds__(kMaxBlock)
 apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
                        const float4* __restrict__ velIn, float4* __restrict__ velOut,
@@ -375,24 +440,44 @@ apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
         if (in_support(c, r2) && fabsf(pj.w) > 1e-8f) {
-            const float rl = sqrtf(r2);
-            const float hr = c.h - rl;
-            const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
             const float4 oj = q.b;
-            const float ol = sqrtf(dot3(oj.x, oj.y, oj.z, oj.x, oj.y, oj.z));
-            ex = ex + ol * g0;
-            ey = ey + ol * g1;
-            ez = ez + ol * g2;
+            if (R) {
+                float w;
+                const float k = spiky_over_r(c, r2, w);
+                const float o2 = fmaf(oj.z, oj.z, fmaf(oj.y, oj.y, oj.x * oj.x));
+                const float s = o2 > 0.0f ? o2 * rsqrtf(o2) * k : 0.0f;
+                ex = fmaf(s, rx, ex);
+                ey = fmaf(s, ry, ey);
+                ez = fmaf(s, rz, ez);
+            } else {
+                const float rl = sqrtf(r2);
+                const float hr = c.h - rl;
+                const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
+                const float ol = sqrtf(dot3(oj.x, oj.y, oj.z, oj.x, oj.y, oj.z));
+                ex = ex + ol * g0;
+                ey = ey + ol * g1;
+                ez = ez + ol * g2;
+            }
         }
     });
     ex = ex * c.negGradSpiky;
     ey = ey * c.negGradSpiky;
     ez = ez * c.negGradSpiky;
-    const float l = sqrtf(dot3(ex, ey, ez, ex, ey, ez));
-    if (l > 0.0f) {
-        ex = ex / l;
-        ey = ey / l;
-        ez = ez / l;
+    if (R) {
+        const float l2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+        if (l2 > 0.0f) {
+            const float w = rsqrtf(l2);
+            ex *= w;
+            ey *= w;
+            ez *= w;
+        }
+    } else {
+        const float l = sqrtf(dot3(ex, ey, ez, ex, ey, ez));
+        if (l > 0.0f) {
+            ex = ex / l;
+            ey = ey / l;
+            ez = ez / l;
+        }
     }
     const float4 oi = omega[i];
     const float fx = c.vort * (ey * oi.z - ez * oi.y);
@@ -436,14 +521,15 @@ void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const
 
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
                             const uint32_t* list, const uint2* meta, int block, cudaStream_t s) {
-    compute_scaling_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, predPacked, density, list, meta);
+    auto k = c.relaxed ? compute_scaling_kernel<true> : compute_scaling_kernel<false>;
+    k<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, predPacked, density, list, meta);
 }
 
 void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, float4* predOut,
                           const float* density, const uint32_t* list, const uint2* meta, int lastIteration,
                           uint8_t* clampMask, int block, cudaStream_t s) {
-    compute_delta_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, b, predPacked, predOut, density, list, meta,
-                                                                  lastIteration, clampMask);
+    auto k = c.relaxed ? compute_delta_kernel<true> : compute_delta_kernel<false>;
+    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, predPacked, predOut, density, list, meta, lastIteration, clampMask);
 }
 
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
@@ -453,12 +539,14 @@ void launch_update_velocities(const DevConsts& c, const float4* pred, const floa
 
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
                             float4* omega, const uint32_t* list, const uint2* meta, int block, cudaStream_t s) {
-    apply_viscosity_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, velIn, velOut, omega, list, meta);
+    auto k = c.relaxed ? apply_viscosity_kernel<true> : apply_viscosity_kernel<false>;
+    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, velIn, velOut, omega, list, meta);
 }
 
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
                             float4* velOut, const uint32_t* list, const uint2* meta, int block, cudaStream_t s) {
-    apply_vorticity_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta);
+    auto k = c.relaxed ? apply_vorticity_kernel<true> : apply_vorticity_kernel<false>;
+    k<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta);
 }
 
 }  // namespace pbf

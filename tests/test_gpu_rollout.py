@@ -5,9 +5,9 @@ Forward: the rollout is the plain substep pipeline, so final positions and
 particle ids are bit-exact against the FP32 oracle.  Backward: the FP32
 adjoint kernels scatter neighbour terms with atomics, so gradients are
 compared with the FP64 adjoint of the same fixed-structure function by
-relative L2 error (ADJ_TOL for the same dL/dx, GRAD_TOL with dL/dx from the
-FP32 forward), and with central differences of the FP64 replay along random
-directions (median within GRAD_TOL).
+relative L2 error (within twice the error of the oracle's serial FP32
+reverse pass, and within GRAD_TOL), and with central differences of the FP64
+replay along random directions (median within GRAD_TOL).
 """
 from __future__ import annotations
 
@@ -18,7 +18,6 @@ pytestmark = pytest.mark.gpu
 
 SUBSTEPS = 10
 GRAD_TOL = 1e-3
-ADJ_TOL = 1e-4
 
 
 def _case(pbf_mod, oracle_mod, seed=11):
@@ -61,21 +60,28 @@ def test_adjoint_matches_fp64_adjoint(pbf_mod, case, cuda_device, every):
     """Same dL/dx in, FP32 GPU adjoint against the FP64 adjoint.  dL/dx is
     taken from the FP64 replay's final positions: the loss residual
     (x - target) is about 1e-4 after a few substeps, so FP32 rounding of the
-    final positions alone would move dL/dx by a few 1e-4 relative."""
+    final positions alone moves dL/dx by a few 1e-4 relative.  The bound is
+    twice the error of the oracle's serial FP32 reverse pass given the same
+    dL/dx (the vorticity direction eta/|eta| is what makes FP32 lose about
+    3e-4 here), and GRAD_TOL."""
     params, pos, vel, R, target = case
     loss64, dv64, dc64, dg64 = R.grad(target)
     _, x64 = R.replay()
+    dldx = _dl_dx(x64, target)
+    _, dv32, dc32, dg32 = R.grad_f32(target, dldx.astype(np.float64))
     with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
         sim.rollout_forward(SUBSTEPS, every)
         x_end = sim.positions_by_id()
-        dv, dc, dg = sim.rollout_backward(_dl_dx(x64, target))
+        dv, dc, dg = sim.rollout_backward(dldx)
         after = sim.positions_by_id()
         own = sim.rollout_backward(_dl_dx(x_end, target))  # the caller's own dL/dx
     np.testing.assert_array_equal(after, x_end)  # the state is left at the end of the rollout
     ev, ec, eg = _rel(dv[:, :3], dv64[:, :3]), abs(dc - dc64) / abs(dc64), _rel(dg, dg64)
-    print(f"checkpoint every {every}: rel err dv0 {ev:.2e}, dc {ec:.2e}, dg {eg:.2e}; "
-          f"with dL/dx from the FP32 forward: dv0 {_rel(own[0][:, :3], dv64[:, :3]):.2e}")
-    assert ev < ADJ_TOL and ec < ADJ_TOL and eg < ADJ_TOL
+    fv, fc, fg = _rel(dv32[:, :3], dv64[:, :3]), abs(dc32 - dc64) / abs(dc64), _rel(dg32, dg64)
+    print(f"checkpoint every {every}: rel err dv0 {ev:.2e}, dc {ec:.2e}, dg {eg:.2e} (serial FP32: {fv:.2e}, "
+          f"{fc:.2e}, {fg:.2e}); with dL/dx from the FP32 forward: dv0 {_rel(own[0][:, :3], dv64[:, :3]):.2e}")
+    for got, f32 in ((ev, fv), (ec, fc), (eg, fg)):
+        assert got < max(2.0 * f32, 1e-5) and got < GRAD_TOL
     assert _rel(own[0][:, :3], dv64[:, :3]) < GRAD_TOL
 
 
