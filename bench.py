@@ -68,7 +68,10 @@ STAGE_BYTES = {
 # compute_scaling_dam_break_1m.md).  Its traffic is dominated by the
 # friend-list rows, so it is scaled to the timed state by the per-particle
 # algorithmic bytes (40 + 4 nl).
-TRAFFIC_CAPTURE = {"kernel": "computeScaling", "bytes": 165.92e6, "nl": 22.3}
+# DRAM bytes (read + write) of one launch from an ncu capture of the
+# dam_break_1m scene after 50 frames, with the mean list length then; scaled
+# to the measured list length by the stage's algorithmic bytes.
+TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 308.16e6, "nl": 31.19}}
 
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -278,9 +281,10 @@ def gpu_arm(args) -> None:
     peak, peak_kind = measured_peaks()
     achieved = algo_bytes / (launch_ms / 1000.0) / 1e9
     traffic = None
-    if dominant == TRAFFIC_CAPTURE["kernel"]:
-        scale = STAGE_BYTES[dominant](nl, nd) / STAGE_BYTES[dominant](TRAFFIC_CAPTURE["nl"], TRAFFIC_CAPTURE["nl"])
-        traffic = TRAFFIC_CAPTURE["bytes"] * scale
+    if dominant in TRAFFIC_CAPTURE:
+        cap = TRAFFIC_CAPTURE[dominant]
+        scale = STAGE_BYTES[dominant](nl, nd) / STAGE_BYTES[dominant](cap["nl"], cap["nl"])
+        traffic = cap["bytes"] * scale
     # ---- the other arithmetic mode, same scene state and block sizes ----
     other = "exact" if args.math == "relaxed" else "relaxed"
     p2 = params.copy()

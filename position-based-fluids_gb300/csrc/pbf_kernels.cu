@@ -161,30 +161,47 @@ build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, cons
     const uint32_t eym = expand_bits(cy - 1) << 1, ey0 = expand_bits(cy) << 1, eyp = expand_bits(cy + 1) << 1;
     const uint32_t ezm = expand_bits(cz - 1) << 2, ez0 = expand_bits(cz) << 2, ezp = expand_bits(cz + 1) << 2;
     const uint32_t base = key_base(b, i);
+    const uint32_t selfHash = pow2 ? ((ex0 | ey0 | ez0) & mask) : ((ex0 | ey0 | ez0) % c.grid);
     uint64_t cnt = 0;  // 8 circles x 8-bit counters
+    auto consider = [&](uint32_t j, const float4 pj) {
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+        if (r2 >= c.h2) return;
+        // thresholds past C-1 are +inf, so only the first C-1 decide
+        int circ = (r2 >= c.circT[0]) + (r2 >= c.circT[1]) + (r2 >= c.circT[2]) + (r2 >= c.circT[3]);
+        if (C > 5) circ += (r2 >= c.circT[4]) + (r2 >= c.circT[5]) + (r2 >= c.circT[6]);
+        const uint32_t k = byte_of(cnt, circ);
+        if ((int)k >= P) return;
+        list[(size_t)(circ * P + (int)k) * n + i] = j;
+        cnt += 1ull << (8 * circ);
+    };
+    // candidates lo .. hi in order, two loads in flight
+    auto scan = [&](uint32_t lo, uint32_t hi) {
+        uint32_t j = lo;
+        for (; j + 1 <= hi; j += 2) {
+            const float4 p0 = __ldg(pred + j), p1 = __ldg(pred + j + 1);
+            consider(j, p0);
+            consider(j + 1, p1);
+        }
+        if (j <= hi) consider(j, __ldg(pred + j));
+    };
     for (int x = -1; x <= 1; ++x) {
         const uint32_t ex = x < 0 ? exm : (x > 0 ? exp_ : ex0);
         for (int y = -1; y <= 1; ++y) {
             const uint32_t exy = ex | (y < 0 ? eym : (y > 0 ? eyp : ey0));
             for (int z = -1; z <= 1; ++z) {
                 const uint32_t m = exy | (z < 0 ? ezm : (z > 0 ? ezp : ez0));
-                const uint2 range = cells[base + (pow2 ? (m & mask) : (m % c.grid))];
+                const uint32_t hm = pow2 ? (m & mask) : (m % c.grid);
+                const uint2 range = cells[base + hm];
                 if (range.x == kEmpty) continue;
                 const uint32_t last = min(range.y, (uint32_t)(n - 1));
                 if (range.x > last) { atomicOr(err, 1); continue; }
-                for (uint32_t j = range.x; j <= last; ++j) {
-                    if ((int)j == i) continue;
-                    const float4 pj = __ldg(pred + j);
-                    const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                    const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-                    if (r2 >= c.h2) continue;
-                    // thresholds past C-1 are +inf, so only the first C-1 decide
-                    int circ = (r2 >= c.circT[0]) + (r2 >= c.circT[1]) + (r2 >= c.circT[2]) + (r2 >= c.circT[3]);
-                    if (C > 5) circ += (r2 >= c.circT[4]) + (r2 >= c.circT[5]) + (r2 >= c.circT[6]);
-                    const uint32_t k = byte_of(cnt, circ);
-                    if ((int)k >= P) continue;
-                    list[(size_t)(circ * P + (int)k) * n + i] = j;
-                    cnt += 1ull << (8 * circ);
+                if (hm == selfHash && range.x <= (uint32_t)i && (uint32_t)i <= last) {
+                    // the particle's own table entry: skip itself (build_friends_list.cl:62)
+                    if ((uint32_t)i > range.x) scan(range.x, (uint32_t)i - 1);
+                    if ((uint32_t)i < last) scan((uint32_t)i + 1, last);
+                } else {
+                    scan(range.x, last);
                 }
             }
         }
