@@ -86,11 +86,38 @@ int pbf_init_buffers(pbf_ctx* ctx, const float* init_pos, const float* init_vel)
    Replaces Simulation::InitCells (src/Simulation.cpp:246-255). */
 int pbf_init_cells(pbf_ctx* ctx);
 
-/* Load the force-plane mask image.  Only mask == NULL (an all-zero mask, for
-   which BouncePointQuad is the identity: compute_delta.cl:33-38) is
-   supported; a non-NULL mask returns PBF_ERR_UNSUPPORTED.
-   Replaces Simulation::LoadForceMasks (src/Simulation.cpp:257-281). */
+/* Load the force-plane mask image: width x height texels, row-major, one
+   uint32 per texel (the R channel the reference keeps, CL_R /
+   CL_UNSIGNED_INT32, with nearest sampling clamped to the edge).  mask ==
+   NULL loads the empty mask, for which every force plane is the identity
+   (compute_delta.cl:33-38).
+   Replaces Simulation::LoadForceMasks (src/Simulation.cpp:257-281), which
+   reads the mask from Scene_fp_mask.png. */
 int pbf_load_force_masks(pbf_ctx* ctx, const uint32_t* mask, int width, int height);
+
+/* Set the force planes of the delta-p stage (at most PBF_MAX_FORCE_QUADS;
+   count 0 removes them).  They are applied in order to the updated position
+   of every particle of every solver iteration, after the position update
+   and before the box clamp, with the reference's noise edge offset
+   1 + (3 + sin(5x/h) + sin(5y/h) + sin(5z/h)) h 0.03 (compute_delta.cl:157-161).
+   The sine is the library's own FP32 definition (the oracle holds the same
+   one), so results are reproducible across host and device.
+   The reference hard-codes its 14 planes (compute_delta.cl:169-182); here
+   they are data.  Rollouts reject contexts with force planes. */
+int pbf_set_force_quads(pbf_ctx* ctx, const PbfForceQuad* quads, int count);
+
+/* The wave generator as a moving wall: with boxClamp, the clamp's low x bound
+   becomes xMin + wavePos for the steps enqueued after this call.  The
+   reference computes wavePos every frame (src/Runner.cpp:100-116) and passes
+   it to computeDelta (src/Simulation.cpp:421, fWavePos), whose kernel does
+   not read it (compute_delta.cl:50).  wavePos must be >= 0. */
+int pbf_set_wave_position(pbf_ctx* ctx, float wavePos);
+
+/* The reference's wave position at `waveTime` seconds of generation
+   (src/Runner.cpp:103-107): (1 - cos(2 pi fmod(waveGenFreq t, 1)^waveGenDuty))
+   * waveGenAmp (xMax - xMin) / 2, evaluated in double.  The caller advances
+   waveTime by timeStep per frame while waves are generated (:110-111). */
+float pbf_wave_position(const PbfParameters* p, float waveTime);
 
 /* Validate the parameters against the allocated buffers and prepare the
    launch plan (sort passes, grid shapes).  Returns PBF_ERR_INVALID where the
@@ -128,6 +155,20 @@ int pbf_synchronize(pbf_ctx* ctx);
    positions (w = density after a step, pack_data.cl with the density source).
    Replaces reading the GL-shared position buffers the renderer draws. */
 int pbf_read_state(pbf_ctx* ctx, float* pos, float* vel, float* pred);
+
+/* Save the particle state (positions, velocities, particle ids, and the
+   parameters it ran with) to a binary file: "PBFSTATE", uint32 version 1,
+   uint32 N, uint32 sizeof(PbfParameters), PbfParameters, N float4
+   positions, N float4 velocities, N uint32 ids, host byte order.  Stepping a
+   context after pbf_load_state of a saved file gives the same results, bit
+   for bit, as stepping the context that saved it.  Replaces the reference's
+   buffer dumps (SaveFile, src/Simulation.cpp:287-313) and its unfinished
+   particle dump (bDumpParticlesData, :605-611). */
+int pbf_save_state(pbf_ctx* ctx, const char* path);
+
+/* Restore a state saved by pbf_save_state into a context with the same N;
+   the context keeps its own parameters. */
+int pbf_load_state(pbf_ctx* ctx, const char* path);
 
 /* Overwrite positions and velocities from host memory (either may be NULL).
    Writing positions renumbers the particles: record k becomes particle k

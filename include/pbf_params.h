@@ -80,6 +80,19 @@ typedef struct PbfParameters {
     int          relaxedMath;
 } PbfParameters;
 
+/* One force plane of the delta-p stage: BouncePointQuad's arguments
+   (compute_delta.cl:1-42), which the reference hard-codes as 14 calls
+   (compute_delta.cl:169-182).  The quad is B + s E0 + t E1 for s, t in
+   [0, 1]; a point that reaches it from the inside is moved onto it where the
+   force mask texel (t * 512, maskYOffset + s * maskHeight) is non-zero. */
+typedef struct PbfForceQuad {
+    float   B[3], E0[3], E1[3];
+    int32_t maskYOffset, maskHeight;
+} PbfForceQuad;
+
+/* Largest number of force planes. */
+#define PBF_MAX_FORCE_QUADS        64
+
 /* Largest friend-circle configuration the kernels accept. */
 #define PBF_MAX_CIRCLES            8
 #define PBF_MAX_PER_CIRCLE         64

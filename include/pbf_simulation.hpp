@@ -66,8 +66,16 @@ public:
         check(pbf_init_cells(mCtx));
     }
 
-    // Simulation::LoadForceMasks (src/Simulation.cpp:257-281): the empty mask.
-    void LoadForceMasks() { check(pbf_load_force_masks(mCtx, nullptr, 0, 0)); }
+    // Simulation::LoadForceMasks (src/Simulation.cpp:257-281): the empty mask,
+    // or `mask` (width x height texels, R channel) where the reference reads
+    // Scene_fp_mask.png.
+    void LoadForceMasks(const uint32_t* mask = nullptr, int width = 0, int height = 0) {
+        check(pbf_load_force_masks(mCtx, mask, width, height));
+    }
+
+    // The force planes the reference hard-codes in computeDelta
+    // (compute_delta.cl:169-182), as data.
+    void SetForceQuads(const PbfForceQuad* quads, int count) { check(pbf_set_force_quads(mCtx, quads, count)); }
 
     // Simulation::InitKernels (src/Simulation.cpp:129-204)
     bool InitKernels() {
@@ -77,17 +85,34 @@ public:
     }
 
     // Simulation::Step (src/Simulation.cpp:554-621): one substep, synchronous.
+    // fWavePos moves the box clamp's low x wall (the reference passes it to
+    // computeDelta, which ignores it); bDumpParticlesData saves the state
+    // after the step to DumpPath (the reference's dump is unfinished,
+    // src/Simulation.cpp:605-611).
     void Step() {
         check(pbf_set_pause(mCtx, bPauseSim ? 1 : 0));
+        if (fWavePos != mWaveSent) {
+            check(pbf_set_wave_position(mCtx, fWavePos));
+            mWaveSent = fWavePos;
+        }
         if (mTrack) check(pbf_enable_stage_timing(mCtx, 1));
         check(pbf_step(mCtx, 1));
         if (mTrack) updateTimings();
+        if (bDumpParticlesData) {
+            bDumpParticlesData = false;
+            SaveState(DumpPath);
+        }
     }
+
+    // Binary particle state (pbf_save_state / pbf_load_state).
+    void SaveState(const std::string& path) { check(pbf_save_state(mCtx, path.c_str())); }
+    void LoadState(const std::string& path) { check(pbf_load_state(mCtx, path.c_str())); }
 
     // Simulation::KernelFileList (src/Simulation.cpp:103-127): the sources
     // the device code is built from.
     const std::string* KernelFileList() {
-        static const std::string files[] = {"pbf_kernels.cu", "pbf_sort.cu", "pbf_capi.cu", ""};
+        static const std::string files[] = {"pbf_kernels.cu", "pbf_sort.cu", "pbf_adjoint.cu", "pbf_capi.cu",
+                                            "pbf_noalloc.cu", ""};
         return files;
     }
 
@@ -109,6 +134,9 @@ public:
     pbf_ctx* handle() const { return mCtx; }
 
     bool bPauseSim = false;
+    float fWavePos = 0.0f;            // src/Simulation.hpp:150
+    bool bDumpParticlesData = false;  // src/Simulation.hpp:149
+    std::string DumpPath = "particles.pbfstate";
     std::vector<PerfTracker> PerfData;
 
 private:
@@ -146,6 +174,7 @@ private:
     }
 
     int mDevice = 0;
+    float mWaveSent = 0.0f;
     pbf_ctx* mCtx = nullptr;
     bool mTrack = false;
 };

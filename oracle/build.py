@@ -65,7 +65,7 @@ def _stale(target: Path, sources: list[Path]) -> bool:
 
 def build_oracle(force: bool = False) -> Path:
     src = HERE / "pbf_oracle.cpp"
-    deps = [src, REPO / "include" / "pbf_params.h"]
+    deps = [src, REPO / "include" / "pbf_params.h", HERE / "noise_sin.hpp"]
     if force or _stale(ORACLE_LIB, deps):
         BUILD.mkdir(exist_ok=True)
         _run(["g++", *CXXFLAGS, "-fopenmp", str(src), "-o", str(ORACLE_LIB)])
@@ -103,7 +103,7 @@ def build_ref(force: bool = False) -> Path | None:
     generated = generate_ref_tu()
     if not generated and not REF_TU.exists():
         return None
-    deps = [REF_TU, HERE / "clshim.hpp", HERE / "ref_driver.inc"]
+    deps = [REF_TU, HERE / "clshim.hpp", HERE / "ref_driver.inc", HERE / "noise_sin.hpp"]
     if force or _stale(REF_LIB, deps):
         _run(["g++", *CXXFLAGS, "-fwrapv", "-w", str(REF_TU), "-o", str(REF_LIB)])
     return REF_LIB

@@ -19,6 +19,7 @@
 // pow with exponent 2 or 3 taken exactly in double and rounded once.
 
 #pragma once
+#include "noise_sin.hpp"
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -115,7 +116,8 @@ inline float length(const float3& a) { return std::sqrt(dot(a, a)); }
 inline float fast_length(const float3& a) { return std::sqrt(dot(a, a)); }
 inline float3 normalize(const float3& a) { return a / length(a); }
 inline float fabs(float v) { return std::fabs(v); }
-inline float sin(float v) { return std::sin(v); }
+// sin: the contract's portable definition (noise_sin.hpp)
+inline float sin(float v) { return noise_sinf_ref(v); }
 inline float max(float a, float b) { return std::fmax(a, b); }
 inline float min(float a, float b) { return std::fmin(a, b); }
 inline int max(int a, int b) { return a > b ? a : b; }

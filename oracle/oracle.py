@@ -52,6 +52,12 @@ def lib() -> ctypes.CDLL:
         l.oracle_rollout_grad_f64.restype = c_double
         l.oracle_rollout_grad_f32.argtypes = [c_void_p] * 8
         l.oracle_rollout_grad_f32.restype = c_double
+        l.oracle_set_force_planes.argtypes = [c_void_p, c_int, c_void_p, c_int, c_int]
+        l.oracle_set_force_planes.restype = c_int
+        l.oracle_set_wave_position.argtypes = [c_float]
+        l.oracle_set_wave_position.restype = None
+        l.oracle_noise_sinf.argtypes = [c_float]
+        l.oracle_noise_sinf.restype = c_float
         _lib = l
     return _lib
 
@@ -71,8 +77,41 @@ def ref() -> ctypes.CDLL:
         l.ref_sort_f32.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]
         l.ref_step_f32.restype = c_int
         l.ref_sort_f32.restype = c_int
+        l.ref_set_force_mask.argtypes = [c_void_p, c_int, c_int]
+        l.ref_set_force_mask.restype = None
         _ref = l
     return _ref
+
+
+# PbfForceQuad (include/pbf_params.h) as a numpy record.
+QUAD_DTYPE = np.dtype([("B", "<f4", 3), ("E0", "<f4", 3), ("E1", "<f4", 3), ("maskYOffset", "<i4"),
+                       ("maskHeight", "<i4")])
+
+
+def set_force_planes(quads=None, mask=None):
+    """Force planes for every later oracle step (None / empty removes them);
+    mask: 2-D uint32 array (rows, width) or None for the empty mask."""
+    q = np.zeros(0, QUAD_DTYPE) if quads is None else np.ascontiguousarray(quads, QUAD_DTYPE)
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint32)
+    rc = lib().oracle_set_force_planes(_ptr(q) if len(q) else None, len(q), _ptr(m),
+                                       0 if m is None else m.shape[1], 0 if m is None else m.shape[0])
+    if rc != 0:
+        raise ValueError("oracle_set_force_planes rejected the planes")
+
+
+def ref_set_force_mask(mask=None):
+    """The mask the shimmed reference computeDelta reads (its 14 planes are in its source)."""
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint32)
+    ref().ref_set_force_mask(_ptr(m), 0 if m is None else m.shape[1], 0 if m is None else m.shape[0])
+
+
+def set_wave_position(wave_pos: float = 0.0) -> None:
+    """The moving wall (xMin + wave_pos) of every later oracle step."""
+    lib().oracle_set_wave_position(float(wave_pos))
+
+
+def noise_sinf(x: float) -> float:
+    return float(lib().oracle_noise_sinf(float(x)))
 
 
 def _ptr(a):

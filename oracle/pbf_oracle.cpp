@@ -40,6 +40,7 @@
 #include <omp.h>
 
 #include "../include/pbf_params.h"
+#include "noise_sin.hpp"
 
 namespace {
 
@@ -323,7 +324,53 @@ template <typename T> void compute_scaling(State<T>& s, const Consts<T>& c) {
     for (int i = 0; i < s.n; ++i) { V4<T> p = s.pred[i]; p.w = s.lambda[i]; s.predP[i] = p; }
 }
 
-// compute_delta.cl:54-185 (with the force planes the identity), then
+// ---- force planes (compute_delta.cl:1-42, 157-182), as data ----
+static std::vector<PbfForceQuad> g_quads;
+static std::vector<uint32_t> g_fmask;
+static int g_fmaskW = 0, g_fmaskH = 0;
+static float g_wave = 0.0f;  // the wave generator's moving wall: xMin + g_wave
+
+template <typename T> T noise_sin(T x) { return (T)std::sin(x); }
+template <> float noise_sin<float>(float x) { return noise_sinf_ref(x); }
+
+// compute_delta.cl:157-161: 1.0 (a double literal) + (3 + sin + sin + sin) h 0.03f.
+template <typename T> T plane_edge_offset(const Consts<T>& c, V3<T> f) {
+    const T nx = f.x * (T)5 / c.h, ny = f.y * (T)5 / c.h, nz = f.z * (T)5 / c.h;
+    const T x = (T)3 + noise_sin(nx) + noise_sin(ny) + noise_sin(nz);
+    return (T)(1.0 + (double)(x * c.h * (T)0.03f));
+}
+
+// BouncePointQuad (compute_delta.cl:1-42).
+template <typename T> V3<T> bounce_point_quad(V3<T> prev, V3<T> next, const PbfForceQuad& q, T edge) {
+    const V3<T> B = {(T)q.B[0], (T)q.B[1], (T)q.B[2]}, E0 = {(T)q.E0[0], (T)q.E0[1], (T)q.E0[2]},
+                E1 = {(T)q.E1[0], (T)q.E1[1], (T)q.E1[2]};
+    const T a = dot(E0, E0), b = dot(E0, E1), c = dot(E1, E1);
+    const T invdet = (T)(1.0 / (double)(a * c - b * b));
+    const V3<T> cr = {E0.y * E1.z - E0.z * E1.y, E0.z * E1.x - E0.x * E1.z, E0.x * E1.y - E0.y * E1.x};
+    const T cl = std::sqrt(dot(cr, cr));
+    const V3<T> n = {cr.x / cl, cr.y / cl, cr.z / cl};
+    const V3<T> ro = {n.x * edge, n.y * edge, n.z * edge};
+    const V3<T> D = {B.x - next.x, B.y - next.y, B.z - next.z};
+    const T e = dot(E1, D), d = dot(E0, D);
+    const T s = invdet * (b * e - c * d), t = invdet * (b * d - a * e);
+    if ((s < 0) || (s > 1) || (t < 0) || (t > 1)) return next;
+    const V3<T> pp = {((B.x + E0.x * s) + E1.x * t) + ro.x, ((B.y + E0.y * s) + E1.y * t) + ro.y,
+                      ((B.z + E0.z * s) + E1.z * t) + ro.z};
+    const V3<T> dP = {next.x - pp.x, next.y - pp.y, next.z - pp.z};
+    if (dot(n, dP) > 0) return next;
+    const T nv = dot(n, V3<T>{prev.x - next.x, prev.y - next.y, prev.z - next.z});
+    if (std::sqrt(dot(dP, dP)) > edge + nv) return next;
+    if (g_fmask.empty()) return next;
+    // (int2)(t * 512.0, maskYOffset + s * maskHeight), clamped to the edge
+    int tx = (int)((double)t * 512.0);
+    int sy = (int)((T)q.maskYOffset + s * (T)q.maskHeight);
+    tx = std::min(std::max(tx, 0), g_fmaskW - 1);
+    sy = std::min(std::max(sy, 0), g_fmaskH - 1);
+    if (g_fmask[(size_t)sy * g_fmaskW + tx] == 0u) return next;
+    return pp;
+}
+
+// compute_delta.cl:54-185 (with the force planes of oracle_set_force_planes), then
 // update_predicted.cl (pred += delta).  The clamp, when enabled, bounds
 // `future` to the box before the delta is formed.
 // `mask` (may be NULL): per particle, which coordinates the clamp moved, two
@@ -357,16 +404,23 @@ template <typename T> void compute_delta(State<T>& s, const Consts<T>& c, uint8_
             }
         V3<T> dp = {(negG * sum.x) / c.rho0, (negG * sum.y) / c.rho0, (negG * sum.z) / c.rho0};
         V3<T> fut = {pi.x + dp.x, pi.y + dp.y, pi.z + dp.z};
+        if (!g_quads.empty()) {
+            const V3<T> prev = {s.pos[i].x, s.pos[i].y, s.pos[i].z};
+            const T edge = plane_edge_offset(c, fut);
+            for (const PbfForceQuad& q : g_quads) fut = bounce_point_quad(prev, fut, q, edge);
+        }
         if (c.clamp) {  // comparisons, so that -0.0 and NaN pass through unchanged
+            T lo[3] = {c.lo[0], c.lo[1], c.lo[2]};
+            if (g_wave != 0.0f) lo[0] = (T)((float)c.lo[0] + g_wave);
             if (mask) {
                 T* f = &fut.x;
                 uint8_t m = 0;
-                for (int k = 0; k < 3; ++k) m |= (uint8_t)((f[k] < c.lo[k] ? 1 : (f[k] > c.hi[k] ? 2 : 0)) << (2 * k));
+                for (int k = 0; k < 3; ++k) m |= (uint8_t)((f[k] < lo[k] ? 1 : (f[k] > c.hi[k] ? 2 : 0)) << (2 * k));
                 mask[i] = m;
             }
-            fut.x = fut.x < c.lo[0] ? c.lo[0] : (fut.x > c.hi[0] ? c.hi[0] : fut.x);
-            fut.y = fut.y < c.lo[1] ? c.lo[1] : (fut.y > c.hi[1] ? c.hi[1] : fut.y);
-            fut.z = fut.z < c.lo[2] ? c.lo[2] : (fut.z > c.hi[2] ? c.hi[2] : fut.z);
+            fut.x = fut.x < lo[0] ? lo[0] : (fut.x > c.hi[0] ? c.hi[0] : fut.x);
+            fut.y = fut.y < lo[1] ? lo[1] : (fut.y > c.hi[1] ? c.hi[1] : fut.y);
+            fut.z = fut.z < lo[2] ? lo[2] : (fut.z > c.hi[2] ? c.hi[2] : fut.z);
         } else if (mask) {
             mask[i] = 0;
         }
@@ -1182,5 +1236,28 @@ double oracle_rollout_grad_f32(void* handle, const double* pos0, const double* v
 uint32_t oracle_grid_hash(int x, int y, int z, uint32_t grid) { return grid_hash(x, y, z, grid); }
 
 int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+// Force planes for every later step (count 0 removes them) and their mask
+// (NULL: the empty mask).  Process-wide state of the oracle.
+int oracle_set_force_planes(const PbfForceQuad* quads, int count, const uint32_t* mask, int w, int h) {
+    if (count < 0 || (count > 0 && !quads)) return -1;
+    g_quads.assign(quads, quads + count);
+    if (mask && w > 0 && h > 0) {
+        g_fmask.assign(mask, mask + (size_t)w * h);
+        g_fmaskW = w;
+        g_fmaskH = h;
+    } else {
+        g_fmask.clear();
+        g_fmaskW = g_fmaskH = 0;
+    }
+    return 0;
+}
+
+// The wave generator's moving wall for every later step: the box clamp's low
+// x bound is xMin + wavePos.
+void oracle_set_wave_position(float wavePos) { g_wave = wavePos; }
+
+// The force planes' noise sine, for the tests.
+float oracle_noise_sinf(float x) { return noise_sinf_ref(x); }
 
 }  // extern "C"

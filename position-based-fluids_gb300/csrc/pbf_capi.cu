@@ -58,6 +58,11 @@ struct pbf_ctx {
     std::vector<PbfParameters> sceneParams;  // empty for a single scene
     std::vector<uint32_t> sceneOffsets;
     pbf::SceneParams* scenes = nullptr;      // device table, batches only
+    float* waveDev = nullptr;                // moving wall offset (pbf_set_wave_position)
+    pbf::QuadDev* quadsDev = nullptr;        // force planes (pbf_set_force_quads)
+    int nquads = 0;
+    uint32_t* maskDev = nullptr;             // force mask (pbf_load_force_masks)
+    int maskW = 0, maskH = 0;
     uint32_t* ids = nullptr;                 // original index of each particle record
     uint32_t* idsTmp = nullptr;
     uint16_t* sceneOf = nullptr;             // device, batches only
@@ -226,6 +231,37 @@ template <typename T> void dev_free(T*& p) {
     p = nullptr;
 }
 
+// Per-plane constants of BouncePointQuad (compute_delta.cl:3-9), in the
+// reference's operation order.
+pbf::QuadDev quad_constants(const PbfForceQuad& in) {
+    pbf::QuadDev q{};
+    for (int k = 0; k < 3; ++k) { q.B[k] = in.B[k]; q.E0[k] = in.E0[k]; q.E1[k] = in.E1[k]; }
+    auto dot = [](const float* u, const float* v) { return (u[0] * v[0] + u[1] * v[1]) + u[2] * v[2]; };
+    q.a = dot(q.E0, q.E0);
+    q.b = dot(q.E0, q.E1);
+    q.c = dot(q.E1, q.E1);
+    q.invdet = (float)(1.0 / (double)(q.a * q.c - q.b * q.b));
+    const float cr[3] = {q.E0[1] * q.E1[2] - q.E0[2] * q.E1[1], q.E0[2] * q.E1[0] - q.E0[0] * q.E1[2],
+                         q.E0[0] * q.E1[1] - q.E0[1] * q.E1[0]};
+    const float len = std::sqrt(dot(cr, cr));
+    for (int k = 0; k < 3; ++k) q.n[k] = cr[k] / len;
+    q.maskYOffset = in.maskYOffset;
+    q.maskHeight = in.maskHeight;
+    return q;
+}
+
+void drop_graph(pbf_ctx* ctx);
+
+// Copies the force planes and mask into the kernel constants.
+void apply_planes(pbf_ctx* ctx) {
+    ctx->consts.nquads = ctx->nquads;
+    ctx->consts.quads = ctx->quadsDev;
+    ctx->consts.mask = ctx->maskDev;
+    ctx->consts.maskW = ctx->maskW;
+    ctx->consts.maskH = ctx->maskH;
+    ctx->consts.wave = ctx->waveDev;
+}
+
 void drop_graph(pbf_ctx* ctx) {
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     ctx->graph = nullptr;
@@ -363,8 +399,9 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
         mark("computeScaling");
         pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, ls.scaling, s);
         mark("computeDelta");
-        pbf::launch_compute_delta(c, b, packed, ctx->pred[a], ctx->density, list, meta, it + 1 == iters,
-                                  tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr, ls.delta, s);
+        pbf::launch_compute_delta(c, b, packed, ctx->pos[sortedPos], ctx->pred[a], ctx->density, list, meta,
+                                  it + 1 == iters, tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr,
+                                  ls.delta, s);
         launched += 2;
     }
     if (iters == 0) {  // packData with the density buffer as it stands (src/Simulation.cpp:591)
@@ -575,6 +612,7 @@ int pbf_destroy(pbf_ctx* ctx) {
     dev_free(ctx->omega); dev_free(ctx->density); dev_free(ctx->hist); dev_free(ctx->cells);
     dev_free(ctx->list); dev_free(ctx->meta); dev_free(ctx->errWord);
     dev_free(ctx->scenes); dev_free(ctx->sceneOf); dev_free(ctx->ids); dev_free(ctx->idsTmp);
+    dev_free(ctx->quadsDev); dev_free(ctx->maskDev); dev_free(ctx->waveDev);
     for (auto& k : ctx->ckpt) { dev_free(k.pos); dev_free(k.vel); dev_free(k.ids); }
     dev_free(ctx->ckptEnd.pos); dev_free(ctx->ckptEnd.vel); dev_free(ctx->ckptEnd.ids);
     free_tape(ctx);
@@ -669,9 +707,135 @@ int pbf_init_cells(pbf_ctx* ctx) {
 
 int pbf_load_force_masks(pbf_ctx* ctx, const uint32_t* mask, int width, int height) {
     if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
-    (void)width; (void)height;
-    if (mask) return fail(ctx, PBF_ERR_UNSUPPORTED, "force-plane masks other than the empty mask are not supported");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!mask) {
+        dev_free(ctx->maskDev);
+        ctx->maskDev = nullptr;
+        ctx->maskW = ctx->maskH = 0;
+    } else {
+        if (width < 1 || height < 1 || (uint64_t)width * (uint64_t)height > (1ull << 28))
+            return fail(ctx, PBF_ERR_INVALID, "pbf_load_force_masks: width and height must be >= 1, at most 2^28 texels");
+        const size_t texels = (size_t)width * height;
+        if (int rc = dev_alloc(ctx, &ctx->maskDev, texels)) return rc;
+        PBF_CUDA(ctx, cudaMemcpy(ctx->maskDev, mask, 4 * texels, cudaMemcpyHostToDevice));
+        ctx->maskW = width;
+        ctx->maskH = height;
+    }
+    drop_graph(ctx);
+    apply_planes(ctx);
     return PBF_OK;
+}
+
+int pbf_set_force_quads(pbf_ctx* ctx, const PbfForceQuad* quads, int count) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    if (count < 0 || count > PBF_MAX_FORCE_QUADS || (count > 0 && !quads))
+        return fail(ctx, PBF_ERR_INVALID, "pbf_set_force_quads: count must be 0 .. PBF_MAX_FORCE_QUADS with quads given");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    dev_free(ctx->quadsDev);
+    ctx->quadsDev = nullptr;
+    ctx->nquads = 0;
+    if (count > 0) {
+        std::vector<pbf::QuadDev> q(count);
+        for (int k = 0; k < count; ++k) q[k] = quad_constants(quads[k]);
+        if (int rc = dev_alloc(ctx, &ctx->quadsDev, (size_t)count)) return rc;
+        PBF_CUDA(ctx, cudaMemcpy(ctx->quadsDev, q.data(), sizeof(pbf::QuadDev) * count, cudaMemcpyHostToDevice));
+        ctx->nquads = count;
+    }
+    drop_graph(ctx);
+    apply_planes(ctx);
+    return PBF_OK;
+}
+
+// ---- state files: "PBFSTATE", version, N, sizeof(PbfParameters), the
+// parameters, then positions, velocities (float4 each) and particle ids, in
+// the current record order, little-endian as the host writes them.
+namespace {
+constexpr char kStateMagic[8] = {'P', 'B', 'F', 'S', 'T', 'A', 'T', 'E'};
+constexpr uint32_t kStateVersion = 1;
+}  // namespace
+
+int pbf_save_state(pbf_ctx* ctx, const char* path) {
+    if (!ctx || !path) return fail(ctx, PBF_ERR_INVALID, "pbf_save_state: NULL argument");
+    if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers has not run");
+    const size_t n = (size_t)ctx->n;
+    std::vector<float> pos(4 * n), vel(4 * n);
+    std::vector<uint32_t> ids(n);
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    PBF_CUDA(ctx, cudaMemcpyAsync(pos.data(), ctx->pos[ctx->curPos], 16 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    PBF_CUDA(ctx, cudaMemcpyAsync(vel.data(), ctx->vel[ctx->curVel], 16 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    PBF_CUDA(ctx, cudaMemcpyAsync(ids.data(), ctx->ids, 4 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(ctx, PBF_ERR_INVALID, std::string("pbf_save_state: cannot open ") + path);
+    const uint32_t head[3] = {kStateVersion, (uint32_t)n, (uint32_t)sizeof(PbfParameters)};
+    bool ok = std::fwrite(kStateMagic, 1, 8, f) == 8 && std::fwrite(head, 4, 3, f) == 3 &&
+              std::fwrite(&ctx->params, sizeof(PbfParameters), 1, f) == 1 &&
+              std::fwrite(pos.data(), 16, n, f) == n && std::fwrite(vel.data(), 16, n, f) == n &&
+              std::fwrite(ids.data(), 4, n, f) == n;
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(ctx, PBF_ERR_INVALID, std::string("pbf_save_state: write failed: ") + path);
+    return PBF_OK;
+}
+
+int pbf_load_state(pbf_ctx* ctx, const char* path) {
+    if (!ctx || !path) return fail(ctx, PBF_ERR_INVALID, "pbf_load_state: NULL argument");
+    if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers has not run");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(ctx, PBF_ERR_INVALID, std::string("pbf_load_state: cannot open ") + path);
+    char magic[8];
+    uint32_t head[3];
+    PbfParameters saved;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kStateMagic, 8) == 0 &&
+              std::fread(head, 4, 3, f) == 3 && head[0] == kStateVersion && head[2] == sizeof(PbfParameters) &&
+              std::fread(&saved, sizeof(PbfParameters), 1, f) == 1;
+    if (!ok) { std::fclose(f); return fail(ctx, PBF_ERR_INVALID, std::string("pbf_load_state: not a state file: ") + path); }
+    if ((int)head[1] != ctx->n) {
+        std::fclose(f);
+        return fail(ctx, PBF_ERR_INVALID, "pbf_load_state: the file holds " + std::to_string(head[1]) +
+                                              " particles, the context " + std::to_string(ctx->n));
+    }
+    const size_t n = (size_t)ctx->n;
+    std::vector<float> pos(4 * n), vel(4 * n);
+    std::vector<uint32_t> ids(n);
+    ok = std::fread(pos.data(), 16, n, f) == n && std::fread(vel.data(), 16, n, f) == n &&
+         std::fread(ids.data(), 4, n, f) == n;
+    std::fclose(f);
+    if (!ok) return fail(ctx, PBF_ERR_INVALID, std::string("pbf_load_state: truncated file: ") + path);
+    std::vector<uint8_t> seen(n, 0);
+    for (uint32_t id : ids) {
+        if (id >= n || seen[id]) return fail(ctx, PBF_ERR_INVALID, "pbf_load_state: particle ids are not a permutation");
+        seen[id] = 1;
+    }
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    PBF_CUDA(ctx, cudaMemcpyAsync(ctx->pos[ctx->curPos], pos.data(), 16 * n, cudaMemcpyHostToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaMemcpyAsync(ctx->vel[ctx->curVel], vel.data(), 16 * n, cudaMemcpyHostToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaMemcpyAsync(ctx->ids, ids.data(), 4 * n, cudaMemcpyHostToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PBF_OK;
+}
+
+int pbf_set_wave_position(pbf_ctx* ctx, float wavePos) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    if (!(wavePos == wavePos) || wavePos < 0.0f) return fail(ctx, PBF_ERR_INVALID, "pbf_set_wave_position: wavePos must be >= 0");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!ctx->waveDev) {
+        if (int rc = dev_alloc(ctx, &ctx->waveDev, 1)) return rc;
+        drop_graph(ctx);  // the kernels now read the wall offset
+        apply_planes(ctx);
+    }
+    // stream-ordered: steps enqueued before see the old wall, steps after the new one
+    PBF_CUDA(ctx, cudaMemcpyAsync(ctx->waveDev, &wavePos, sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PBF_OK;
+}
+
+// src/Runner.cpp:100-116
+float pbf_wave_position(const PbfParameters* p, float waveTime) {
+    if (!p) return 0.0f;
+    const double push = (double)p->waveGenAmp * ((double)p->xMax - (double)p->xMin);
+    const double t = (double)p->waveGenFreq * (double)waveTime;
+    const double phase = std::pow(std::fmod(t, 1.0), (double)p->waveGenDuty);
+    return (float)((1.0 - std::cos(2.0 * 3.14159265358979323846 * phase)) * push / 2.0);
 }
 
 int pbf_init_kernels(pbf_ctx* ctx) {
@@ -686,6 +850,7 @@ int pbf_init_kernels(pbf_ctx* ctx) {
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
     drop_graph(ctx);
     ctx->consts = pbf::make_consts(ctx->params, ctx->n);
+    apply_planes(ctx);
     uint64_t keyRange = ctx->params.gridBufSize;
     if (is_batch(ctx)) {
         const size_t S = ctx->sceneParams.size();
@@ -719,6 +884,7 @@ int pbf_set_params(pbf_ctx* ctx, const PbfParameters* params) {
     if (ctx->kernelsReady) {
         drop_graph(ctx);
         ctx->consts = pbf::make_consts(ctx->params, ctx->n);
+        apply_planes(ctx);
     }
     return PBF_OK;
 }
@@ -1016,6 +1182,7 @@ int pbf_rollout_forward(pbf_ctx* ctx, int substeps, int checkpoint_every) {
     if (rc) return rc;
     if (is_batch(ctx)) return fail(ctx, PBF_ERR_UNSUPPORTED, "rollouts run on single-scene contexts");
     if (ctx->paused) return fail(ctx, PBF_ERR_STATE, "rollouts need an unpaused simulation");
+    if (ctx->nquads > 0) return fail(ctx, PBF_ERR_UNSUPPORTED, "rollouts do not differentiate force planes");
     if (substeps < 1 || checkpoint_every < 1) return fail(ctx, PBF_ERR_INVALID, "substeps and checkpoint_every must be >= 1");
     if (ctx->params.simIterations < 1 || ctx->params.simIterations > 64)
         return fail(ctx, PBF_ERR_INVALID, "rollouts need 1..64 solver iterations");

@@ -13,6 +13,16 @@ namespace pbf {
 // Constants every solver kernel reads, formed once on the host from the
 // parameters (src/Simulation.cpp:169-183 bakes the same values into the
 // OpenCL build as -D literals).
+// One force plane with its per-plane constants formed on the host
+// (compute_delta.cl:3-9): a, b, c, invdet = 1.0 / (a c - b b) taken in
+// double and rounded once (the literal 1.0 is a double), and
+// planeNorm = normalize(cross(E0, E1)) as cross / sqrt(dot).
+struct QuadDev {
+    float B[3], E0[3], E1[3], n[3];
+    float a, b, c, invdet;
+    int maskYOffset, maskHeight;
+};
+
 struct DevConsts {
     float dt, h, h2, minR, hMinusMinR;
     float poly6, gradSpiky, negGradSpiky, poly6q;
@@ -21,6 +31,10 @@ struct DevConsts {
     float lo[3], hi[3];
     int clamp, guard;
     int relaxed;                 // relaxedMath: the neighbour passes' relaxed variants
+    int nquads, maskW, maskH;    // force planes (pbf_set_force_quads) and their mask
+    const QuadDev* quads;
+    const uint32_t* mask;        // NULL: the empty mask
+    const float* wave;           // device scalar: the moving wall's offset from xMin (NULL: none)
     float dpScale, invPoly6q;    // -gradSpiky / rho0 and 1 / poly6q (relaxed variants only)
     int circles, perCircle;
     uint32_t grid;
@@ -74,9 +88,10 @@ void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const
                           uint2* meta, int* errorWord, int block, cudaStream_t s);
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
                             const uint32_t* list, const uint2* meta, int block, cudaStream_t s);
-void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, float4* predOut,
-                          const float* density, const uint32_t* list, const uint2* meta, int lastIteration,
-                          uint8_t* clampMask, int block, cudaStream_t s);
+// posPrev: the sorted positions, read only by the force planes.
+void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, const float4* posPrev,
+                          float4* predOut, const float* density, const uint32_t* list, const uint2* meta,
+                          int lastIteration, uint8_t* clampMask, int block, cudaStream_t s);
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
                               float4* vel, const uint32_t* idsIn, uint32_t* idsOut, cudaStream_t s);
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,

@@ -289,8 +289,8 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
 // src/Simulation.cpp:591).
 template <bool R>
 __global__ void __launch_bounds__(kMaxBlock)
-compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, float4* __restrict__ predOut,
-                     const float* __restrict__ density, const uint32_t* __restrict__ list,
+compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const float4* __restrict__ posPrev,
+                     float4* __restrict__ predOut, const float* __restrict__ density, const uint32_t* __restrict__ list,
                      const uint2* __restrict__ meta, int lastIteration, uint8_t* __restrict__ clampMask) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
@@ -342,6 +342,11 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, float4
         fy = pi.y + (c.negGradSpiky * sy) / c.rho0;
         fz = pi.z + (c.negGradSpiky * sz) / c.rho0;
     }
+    if (c.nquads > 0) {  // force planes, in order (compute_delta.cl:157-182)
+        const float4 prev = posPrev[i];
+        const float edge = plane_edge_offset(c, fx, fy, fz);
+        for (int q = 0; q < c.nquads; ++q) bounce_point_quad(c, c.quads[q], prev.x, prev.y, prev.z, fx, fy, fz, edge);
+    }
     if (c.clamp) {
         const float* lo = c.lo;
         const float* hi = c.hi;
@@ -350,10 +355,12 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, float4
             lo = sp.lo;
             hi = sp.hi;
         }
+        // the wave generator's moving wall: xMin + wavePos (pbf_set_wave_position)
+        const float lx = c.wave ? lo[0] + *c.wave : lo[0];
         if (clampMask)  // which coordinates the clamp moves: 2 bits per axis, 1 low, 2 high
-            clampMask[i] = (uint8_t)((fx < lo[0] ? 1 : (fx > hi[0] ? 2 : 0)) | (fy < lo[1] ? 4 : (fy > hi[1] ? 8 : 0)) |
+            clampMask[i] = (uint8_t)((fx < lx ? 1 : (fx > hi[0] ? 2 : 0)) | (fy < lo[1] ? 4 : (fy > hi[1] ? 8 : 0)) |
                                      (fz < lo[2] ? 16 : (fz > hi[2] ? 32 : 0)));
-        fx = fx < lo[0] ? lo[0] : (fx > hi[0] ? hi[0] : fx);
+        fx = fx < lx ? lx : (fx > hi[0] ? hi[0] : fx);
         fy = fy < lo[1] ? lo[1] : (fy > hi[1] ? hi[1] : fy);
         fz = fz < lo[2] ? lo[2] : (fz > hi[2] ? hi[2] : fz);
     } else if (clampMask) {
@@ -542,11 +549,12 @@ void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* pred
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, predPacked, density, list, meta);
 }
 
-void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, float4* predOut,
-                          const float* density, const uint32_t* list, const uint2* meta, int lastIteration,
-                          uint8_t* clampMask, int block, cudaStream_t s) {
+void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, const float4* posPrev,
+                          float4* predOut, const float* density, const uint32_t* list, const uint2* meta,
+                          int lastIteration, uint8_t* clampMask, int block, cudaStream_t s) {
     auto k = c.relaxed ? compute_delta_kernel<true> : compute_delta_kernel<false>;
-    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, predPacked, predOut, density, list, meta, lastIteration, clampMask);
+    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, predPacked, posPrev, predOut, density, list, meta, lastIteration,
+                                               clampMask);
 }
 
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,

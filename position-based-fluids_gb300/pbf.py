@@ -59,6 +59,11 @@ class PbfParameters(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+# PbfForceQuad (include/pbf_params.h) as a numpy record.
+QUAD_DTYPE = np.dtype([("B", "<f4", 3), ("E0", "<f4", 3), ("E1", "<f4", 3), ("maskYOffset", "<i4"),
+                       ("maskHeight", "<i4")])
+
+
 class PbfError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"[{code}] {message}")
@@ -112,6 +117,10 @@ def library() -> ctypes.CDLL:
         "pbf_set_launch_shape": [c_void_p, POINTER(c_int)],
         "pbf_autotune": [c_void_p, c_int, POINTER(c_int)],
         "pbf_read_ids": [c_void_p, u32p],
+        "pbf_set_force_quads": [c_void_p, c_void_p, c_int],
+        "pbf_set_wave_position": [c_void_p, c_float],
+        "pbf_save_state": [c_void_p, ctypes.c_char_p],
+        "pbf_load_state": [c_void_p, ctypes.c_char_p],
         "pbf_rollout_forward": [c_void_p, c_int, c_int],
         "pbf_rollout_backward": [c_void_p, f32p, f32p, POINTER(c_float), f32p],
     }
@@ -121,6 +130,8 @@ def library() -> ctypes.CDLL:
         fn.restype = c_int
     lib.pbf_last_error.argtypes = [c_void_p]
     lib.pbf_last_error.restype = c_char_p
+    lib.pbf_wave_position.argtypes = [P, c_float]
+    lib.pbf_wave_position.restype = c_float
     _lib = lib
     return lib
 
@@ -172,6 +183,11 @@ def sort_state_noalloc(params: PbfParameters, d_pred: int, d_keys: int, d_perm: 
                        stream: int | None = None) -> None:
     """pbf_sort_state_noalloc on device addresses (see include/pbf_capi.h)."""
     _check(library().pbf_sort_state_noalloc(ctypes.byref(params), d_pred, d_keys, d_perm, d_cells, stream))
+
+
+def wave_position(params: PbfParameters, wave_time: float) -> float:
+    """The reference's wave position after `wave_time` seconds (src/Runner.cpp:103-107)."""
+    return float(library().pbf_wave_position(ctypes.byref(params), float(wave_time)))
 
 
 def reference_lattice(params: PbfParameters) -> np.ndarray:
@@ -348,6 +364,20 @@ class Simulation:
     def use_graph(self, on: bool) -> None:
         _check(self.lib.pbf_use_graph(self._ctx, int(on)), self._ctx)
 
+    def set_force_quads(self, quads) -> None:
+        """Force planes: a numpy array of QUAD_DTYPE records (PbfForceQuad)."""
+        q = np.ascontiguousarray(quads, QUAD_DTYPE) if quads is not None else np.zeros(0, QUAD_DTYPE)
+        _check(self.lib.pbf_set_force_quads(self._ctx, q.ctypes.data if len(q) else None, len(q)), self._ctx)
+
+    def set_wave_position(self, wave_pos: float) -> None:
+        _check(self.lib.pbf_set_wave_position(self._ctx, float(wave_pos)), self._ctx)
+
+    def save_state(self, path) -> None:
+        _check(self.lib.pbf_save_state(self._ctx, str(path).encode()), self._ctx)
+
+    def load_state(self, path) -> None:
+        _check(self.lib.pbf_load_state(self._ctx, str(path).encode()), self._ctx)
+
     def read_ids(self) -> np.ndarray:
         ids = np.empty(self.n, np.uint32)
         _check(self.lib.pbf_read_ids(self._ctx, _u32(ids)), self._ctx)
@@ -401,7 +431,8 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_enable_stage_timing", "pbf_stage_timings", "pbf_launch_count", "pbf_use_graph",
         "pbf_reference_lattice", "pbf_scene_block", "pbf_sort_state_noalloc", "pbf_scene_double_dam_break",
         "pbf_create_batch", "pbf_scene_offsets", "pbf_get_launch_shape", "pbf_set_launch_shape", "pbf_autotune",
-        "pbf_read_ids", "pbf_rollout_forward", "pbf_rollout_backward",
+        "pbf_read_ids", "pbf_rollout_forward", "pbf_rollout_backward", "pbf_set_force_quads",
+        "pbf_set_wave_position", "pbf_wave_position", "pbf_save_state", "pbf_load_state",
     ])
 
 

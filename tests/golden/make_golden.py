@@ -52,6 +52,49 @@ CASES = [
 ]
 SEED = 20240601
 
+# Force planes: the reference's 14 BouncePointQuad calls are read from its
+# computeDelta source and stored as data; a 4,096-particle block falls onto
+# plane 7 (a floor at y = -41.65, normal +y) through a mask with holes.
+FORCE_CASE = {"name": "force_planes_4k_4sub", "block": [16, 16, 16], "origin": [-62.0, -40.9, -1.0],
+              "substeps": 4, "mask": {"width": 512, "height": 9262, "rule": "0 where (x // 8 + y // 4) % 3 == 0, else 1"}}
+
+
+def reference_force_quads():
+    """The 14 planes hard-coded in the reference (compute_delta.cl:169-182)."""
+    import re
+    src = (oracle._build.REFERENCE / "assets" / "kernels" / "compute_delta.cl").read_text()
+    vec = r"\(float3\)\(\s*([-0-9.eE]+),\s*([-0-9.eE]+),\s*([-0-9.eE]+)\)"
+    pat = re.compile(r"BouncePointQuad\(positions\[i\]\.xyz, future, " + vec + r", " + vec + r", " + vec +
+                     r", surfacesMask, (\d+), (\d+), edgeOffset\)")
+    quads = []
+    for m in pat.finditer(src):
+        v = [float(x) for x in m.groups()[:9]]
+        quads.append({"B": v[0:3], "E0": v[3:6], "E1": v[6:9], "maskYOffset": int(m.group(10)),
+                      "maskHeight": int(m.group(11))})
+    return quads
+
+
+def force_mask(spec):
+    y, x = np.mgrid[0:spec["height"], 0:spec["width"]]
+    return np.where((x // 8 + y // 4) % 3 == 0, 0, 1).astype(np.uint32)
+
+
+def quads_array(quads):
+    a = np.zeros(len(quads), oracle.QUAD_DTYPE)
+    for k, q in enumerate(quads):
+        a[k] = (q["B"], q["E0"], q["E1"], q["maskYOffset"], q["maskHeight"])
+    return a
+
+
+def force_scene():
+    params = pbf.load_scenario("dam_break_32k")
+    params.boxClamp = 0
+    params.zeroDistanceGuard = 0
+    dims = FORCE_CASE["block"]
+    params.particleCount = dims[0] * dims[1] * dims[2]
+    pos = pbf.scene_block(*dims, 0.05, tuple(FORCE_CASE["origin"]), 0.005, SEED)
+    return params, pos, np.zeros_like(pos)
+
 
 def scene(dims, overrides):
     params = pbf.load_scenario(overrides.get("base", "dam_break_32k"))
@@ -105,6 +148,19 @@ def main() -> None:
         if name == "small_2k_2sub":
             np.savez_compressed(OUT / "small_case.npz", init_pos=pos, **arrays)
         print(f"{name}: n={params.particleCount} substeps={substeps}")
+    quads = reference_force_quads()
+    assert len(quads) == 14, len(quads)
+    params, pos, vel = force_scene()
+    oracle.ref_set_force_mask(force_mask(FORCE_CASE["mask"]))
+    try:
+        p, v, pr, keys, perm, cells = oracle.ref_step(params, pos, vel, FORCE_CASE["substeps"])
+    finally:
+        oracle.ref_set_force_mask(None)
+    arrays = {"pos": p, "vel": v, "pred": pr, "keys": keys, "perm": perm, "cells": cells}
+    manifest["force_planes"] = dict(FORCE_CASE, quads=quads, sha256={k: digest(a) for k, a in arrays.items()},
+                                    source="reference assets/kernels/compute_delta.cl:169-182")
+    moved = float(np.mean(np.abs(p[:, 1] - pos[:, 1]) > 0))
+    print(f"{FORCE_CASE['name']}: n={params.particleCount}, min y {p[:, 1].min():.3f}, nan {int(np.isnan(p).sum())}")
     (OUT / "golden.json").write_text(json.dumps(manifest, indent=1) + "\n")
 
 

@@ -246,10 +246,35 @@ def test_argument_errors(pbf_mod, cuda_device):
         with pytest.raises(pbf_mod.PbfError):
             sim.set_params(bad)
         with pytest.raises(pbf_mod.PbfError) as e:
-            sim.LoadForceMasks(np.ones((4, 4), np.uint32))
-        assert e.value.code == pbf_mod.PBF_ERR_UNSUPPORTED
+            sim.LoadForceMasks(np.ones((0, 4), np.uint32))  # an empty image
+        assert e.value.code == pbf_mod.PBF_ERR_INVALID
+        with pytest.raises(pbf_mod.PbfError):
+            sim.set_wave_position(-1.0)
     s = pbf_mod.Simulation(params, cuda_device)
     with pytest.raises(pbf_mod.PbfError) as e:
         s.Step(1)
     assert e.value.code == pbf_mod.PBF_ERR_STATE
     s.close()
+
+
+def test_force_planes_match_reference_digests(pbf_mod, cuda_device):
+    """The reference's 14 force planes as data (pbf_set_force_quads) with a
+    mask (pbf_load_force_masks): bit-exact against the reference's own
+    computeDelta with its hard-coded planes."""
+    manifest = json.loads((GOLDEN / "golden.json").read_text())
+    force = manifest["force_planes"]
+    params, pos, vel = mg().force_scene()
+    quads = mg().quads_array(force["quads"])
+    with pbf_mod.Simulation(params, cuda_device) as sim:
+        sim.InitBuffers(pos, vel)
+        sim.InitCells()
+        sim.LoadForceMasks(mg().force_mask(force["mask"]))
+        sim.InitKernels()
+        sim.set_force_quads(quads)
+        sim.Step(force["substeps"])
+        p, v, pr = sim.read_state()
+        sim.set_force_quads(None)   # removing the planes restores the plain path
+        with pytest.raises(pbf_mod.PbfError):
+            sim.set_force_quads(np.zeros(65, pbf_mod.QUAD_DTYPE))
+    for name, arr in (("pos", p), ("vel", v), ("pred", pr)):
+        assert mg().digest(arr) == force["sha256"][name], name

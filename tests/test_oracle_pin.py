@@ -123,3 +123,68 @@ def test_fp64_oracle_close_to_fp32(pbf_mod, oracle_mod):
     p64, v64, _ = oracle_mod.step_f64(params, pos, vel, 1)
     assert np.max(np.abs(p32[:, :3] - p64[:, :3])) < 1e-5
     assert np.max(np.abs(v32[:, :3] - v64[:, :3])) < 5e-3
+
+
+# ---- force planes (compute_delta.cl:1-42, 157-182) ----
+
+FORCE = MANIFEST["force_planes"]
+
+
+def _force_setup():
+    mg = _make_golden()
+    params, pos, vel = mg.force_scene()
+    return mg, params, pos, vel, mg.quads_array(FORCE["quads"]), mg.force_mask(FORCE["mask"])
+
+
+def test_force_planes_are_the_reference_planes():
+    """golden.json holds the reference's 14 hard-coded planes as data."""
+    assert len(FORCE["quads"]) == 14
+    assert FORCE["quads"][7]["maskYOffset"] == 3578 and FORCE["quads"][7]["maskHeight"] == 369
+
+
+def test_oracle_force_planes_match_reference_digests(pbf_mod, oracle_mod):
+    mg, params, pos, vel, quads, mask = _force_setup()
+    oracle_mod.set_force_planes(quads, mask)
+    try:
+        p, v, pr, dbg = oracle_mod.step(params, pos, vel, FORCE["substeps"], debug=True)
+        p0, _, _ = oracle_mod.step(params, pos, vel, 1)
+    finally:
+        oracle_mod.set_force_planes(None, None)
+    got = {"pos": p, "vel": v, "pred": pr, "keys": dbg["keys"], "perm": dbg["perm"], "cells": dbg["cells"]}
+    for k, want in FORCE["sha256"].items():
+        assert _digest(got[k]) == want, f"force planes: {k} differs from the reference kernels"
+    q0, _, _ = oracle_mod.step(params, pos, vel, 1)  # without planes
+    assert not np.array_equal(p0, q0), "the planes act on this scene"
+
+
+@pytest.mark.skipif(not __import__("oracle.oracle", fromlist=["x"]).ref_available(),
+                    reason="the reference's kernels are not available here")
+def test_oracle_force_planes_match_reference_live(pbf_mod, oracle_mod):
+    """Another mask (holes in the other texels) and two substeps, against the
+    reference's computeDelta with its own hard-coded planes."""
+    mg, params, pos, vel, quads, mask = _force_setup()
+    mask = (1 - mask).astype(np.uint32)
+    oracle_mod.set_force_planes(quads, mask)
+    oracle_mod.ref_set_force_mask(mask)
+    try:
+        a = oracle_mod.step(params, pos, vel, 2)
+        b = oracle_mod.ref_step(params, pos, vel, 2)
+    finally:
+        oracle_mod.set_force_planes(None, None)
+        oracle_mod.ref_set_force_mask(None)
+    for x, y, name in zip(a, b[:3], ("pos", "vel", "pred")):
+        assert np.array_equal(mg.canonical(x).view(np.uint32), mg.canonical(y).view(np.uint32)), name
+
+
+def test_noise_sine_accuracy(oracle_mod):
+    """The planes' portable FP32 sine against the FP64 sine: a few ulp over
+    the range the noise offset sees, exact at the quadrant points."""
+    rng = np.random.default_rng(3)
+    xs = np.concatenate([rng.uniform(-3000.0, 3000.0, 20000), rng.uniform(-4.0, 4.0, 5000)]).astype(np.float32)
+    got = np.array([oracle_mod.noise_sinf(float(x)) for x in xs], np.float32)
+    want = np.sin(xs.astype(np.float64))
+    ulp = np.spacing(np.maximum(np.abs(want), 2.0 ** -24).astype(np.float32)).astype(np.float64)
+    err = np.abs(got.astype(np.float64) - want) / ulp
+    print(f"noise sine: max error {err.max():.2f} ulp, mean {err.mean():.3f}")
+    assert err.max() <= 4.0
+    assert oracle_mod.noise_sinf(0.0) == 0.0 and np.isnan(oracle_mod.noise_sinf(float("nan")))

@@ -106,3 +106,15 @@ def test_constants_follow_reference_literals(pbf_mod, oracle_mod):
     qh = np.float32(np.float32(0.2) * np.float32(0.1))
     d = np.float32(p.h_2 - np.float32(float(qh) * float(qh)))
     assert poly6q == np.float32(float(d) ** 3)
+
+
+def test_wave_position_follows_the_runner_formula(pbf_mod):
+    """pbf_wave_position: (1 - cos(2 pi fmod(f t, 1)^duty)) amp (xMax - xMin) / 2
+    (src/Runner.cpp:103-107)."""
+    import math
+    p = pbf_mod.load_scenario("dam_break_32k")
+    p.waveGenAmp, p.waveGenFreq, p.waveGenDuty = 0.2, 0.7, 1.5
+    for t in (0.0, 0.3, 1.1, 2.9):
+        want = (1 - math.cos(2 * math.pi * math.fmod(0.7 * float(np.float32(t)), 1.0) ** 1.5)) * \
+            0.2 * (p.xMax - p.xMin) / 2
+        assert abs(pbf_mod.wave_position(p, t) - want) <= 1e-6 * max(1.0, abs(want))
