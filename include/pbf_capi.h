@@ -216,6 +216,32 @@ int pbf_enable_stage_timing(pbf_ctx* ctx, int enable);
 int pbf_stage_timings(pbf_ctx* ctx, float* ms, int capacity, int* count,
                       char* names, size_t names_len);
 
+/* One performance tracker, the fields of the reference's
+   PM_PERFORMANCE_TRACKER (src/OCLPerfMon.h) without the OpenCL event.
+   Trackers are named as OCLPerfMon::GetTrackerEvent names them: the stage,
+   with "_<iteration>" for the per-iteration stages (computeScaling_0, ...).
+   A stage here may cover several reference kernels: predictPositions also
+   computes the keys, radixsort is the whole sort, computeScaling_i includes
+   packData_i and computeDelta_i includes updatePredicted_i. */
+typedef struct PbfPerfTracker {
+    char     eventName[48];
+    uint64_t time_start;  /* ns since pbf_enable_stage_timing turned timing on */
+    uint64_t time_end;
+    double   total_time;  /* ms: current * 0.5 + last_time * 0.5 (OCLPerfMon::UpdateTimings) */
+    double   last_time;   /* ms */
+} PbfPerfTracker;
+
+/* The trackers in order of first use (the order the reference's UI draws
+   them, src/UIManager.cpp:185-215), updated after every timed step.
+   Replaces PerfData.Trackers (src/Simulation.hpp, OCLPerfMon). */
+int pbf_perf_trackers(pbf_ctx* ctx, PbfPerfTracker* out, int capacity, int* count);
+
+/* The trackers as one JSON object for dashboards: {"trackers": [{"eventName",
+   "time_start", "time_end", "total_time", "last_time"}, ...], "total_time",
+   "unit": "ms"}.  *length receives the size needed including the NUL; buf
+   (capacity bytes) receives as much as fits. */
+int pbf_perf_export_json(pbf_ctx* ctx, char* buf, size_t capacity, size_t* length);
+
 /* Number of kernels this context has launched so far (graph nodes counted
    one by one). */
 int pbf_launch_count(pbf_ctx* ctx, uint64_t* count);

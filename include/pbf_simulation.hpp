@@ -16,6 +16,7 @@
 // Header-only over include/pbf_capi.h; link with libpbf_gb300.so.
 #pragma once
 
+#include <deque>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -36,10 +37,45 @@ inline void LoadParameters(std::string fileContents) {
     ParametersChanged = true;
 }
 
-// Per-stage device times, in the reference tracker names (src/OCLPerfMon.h).
-struct PerfTracker {
+// src/OCLPerfMon.h: one performance tracker (without the cl::Event), and the
+// monitor whose Trackers vector the reference's UI reads
+// (src/UIManager.cpp:185-215, 336-345).
+typedef struct {
     std::string eventName;
-    double total_time;  // milliseconds, exponentially smoothed with weight 0.5
+    uint64_t time_start;  // [nano sec]
+    uint64_t time_end;    // [nano sec]
+    double total_time;    // [millisec]
+    double last_time;     // [millisec]
+    int Tag;
+} PM_PERFORMANCE_TRACKER;
+
+class OCLPerfMon {
+public:
+    std::vector<PM_PERFORMANCE_TRACKER*> Trackers;
+
+    // OCLPerfMon::UpdateTimings: here the library keeps the smoothed times;
+    // this copies them in (pbf_perf_trackers).
+    void UpdateTimings(pbf_ctx* ctx) {
+        int count = 0;
+        if (pbf_perf_trackers(ctx, nullptr, 0, &count) != PBF_OK) return;
+        std::vector<PbfPerfTracker> t((size_t)count);
+        if (count && pbf_perf_trackers(ctx, t.data(), count, &count) != PBF_OK) return;
+        while (mStore.size() < t.size()) {
+            mStore.push_back(PM_PERFORMANCE_TRACKER{});
+            Trackers.push_back(&mStore.back());
+        }
+        for (size_t i = 0; i < t.size(); ++i) {
+            PM_PERFORMANCE_TRACKER& p = mStore[i];
+            p.eventName = t[i].eventName;
+            p.time_start = t[i].time_start;
+            p.time_end = t[i].time_end;
+            p.total_time = t[i].total_time;
+            p.last_time = t[i].last_time;
+        }
+    }
+
+private:
+    std::deque<PM_PERFORMANCE_TRACKER> mStore;  // stable addresses for Trackers
 };
 
 class Simulation {
@@ -97,7 +133,7 @@ public:
         }
         if (mTrack) check(pbf_enable_stage_timing(mCtx, 1));
         check(pbf_step(mCtx, 1));
-        if (mTrack) updateTimings();
+        if (mTrack) PerfData.UpdateTimings(mCtx);
         if (bDumpParticlesData) {
             bDumpParticlesData = false;
             SaveState(DumpPath);
@@ -137,7 +173,7 @@ public:
     float fWavePos = 0.0f;            // src/Simulation.hpp:150
     bool bDumpParticlesData = false;  // src/Simulation.hpp:149
     std::string DumpPath = "particles.pbfstate";
-    std::vector<PerfTracker> PerfData;
+    OCLPerfMon PerfData;
 
 private:
     void check(int rc, pbf_ctx* ctx) const {
@@ -149,28 +185,6 @@ private:
         if (!mCtx) throw std::runtime_error("InitBuffers must run first");
         int rc = pbf_set_params(mCtx, &Params);
         if (strict) check(rc);
-    }
-
-    // OCLPerfMon::UpdateTimings (src/OCLPerfMon.cpp:36-51): EMA with weight 0.5.
-    void updateTimings() {
-        float ms[64];
-        int count = 0;
-        char names[2048];
-        check(pbf_stage_timings(mCtx, ms, 64, &count, names, sizeof names));
-        std::vector<std::string> keys;
-        std::string all(names), cur;
-        for (char ch : all) {
-            if (ch == '\n') { keys.push_back(cur); cur.clear(); }
-            else cur += ch;
-        }
-        if (!cur.empty()) keys.push_back(cur);
-        for (int k = 0; k < count && k < (int)keys.size(); ++k) {
-            PerfTracker* t = nullptr;
-            for (auto& e : PerfData)
-                if (e.eventName == keys[k]) t = &e;
-            if (!t) { PerfData.push_back({keys[k], 0.0}); t = &PerfData.back(); }
-            t->total_time = ms[k] * 0.5 + t->total_time * 0.5;
-        }
     }
 
     int mDevice = 0;

@@ -82,6 +82,9 @@ struct pbf_ctx {
     bool stageTiming = false;
     std::vector<std::string> stageNames;
     std::vector<float> stageMs;
+    // per-launch trackers in the reference's naming (OCLPerfMon), EMA 0.5
+    std::vector<PbfPerfTracker> trackers;
+    cudaEvent_t timingAnchor = nullptr;  // time zero of the trackers' timestamps
 
     // rollout: state at the start of every segment of `rollEvery` substeps,
     // and at the end (pbf_rollout_forward / pbf_rollout_backward)
@@ -311,17 +314,35 @@ int check_batch_compatible(pbf_ctx* ctx, const std::vector<PbfParameters>& sp) {
 // ------------------------------------------------------------- the step --
 struct StageClock {
     pbf_ctx* ctx;
-    std::vector<std::pair<int, cudaEvent_t>> marks;  // (stage index, event recorded before it)
-    int stage(const char* name) {
+    struct Mark {
+        int stage;      // index into stageNames (the base name)
+        int tracker;    // index into trackers (the name with its iteration suffix)
+        cudaEvent_t event;
+    };
+    std::vector<Mark> marks;
+    // `iteration` >= 0 names the tracker name_iteration, as
+    // OCLPerfMon::GetTrackerEvent(name, iterationIndex) does (src/OCLPerfMon.cpp:3-31).
+    int stage(const char* name, int iteration = -1) {
         if (!ctx->stageTiming) return PBF_OK;
         int idx = -1;
         for (size_t k = 0; k < ctx->stageNames.size(); ++k)
             if (ctx->stageNames[k] == name) idx = (int)k;
         if (idx < 0) { ctx->stageNames.push_back(name); ctx->stageMs.push_back(0.0f); idx = (int)ctx->stageNames.size() - 1; }
+        std::string tname = name;
+        if (iteration >= 0) tname += "_" + std::to_string(iteration);
+        int tidx = -1;
+        for (size_t k = 0; k < ctx->trackers.size(); ++k)
+            if (tname == ctx->trackers[k].eventName) tidx = (int)k;
+        if (tidx < 0) {
+            PbfPerfTracker t{};
+            std::snprintf(t.eventName, sizeof t.eventName, "%s", tname.c_str());
+            ctx->trackers.push_back(t);
+            tidx = (int)ctx->trackers.size() - 1;
+        }
         cudaEvent_t e;
         PBF_CUDA(ctx, cudaEventCreate(&e));
         PBF_CUDA(ctx, cudaEventRecord(e, ctx->stream));
-        marks.emplace_back(idx, e);
+        marks.push_back({idx, tidx, e});
         return PBF_OK;
     }
     int finish() {
@@ -331,12 +352,22 @@ struct StageClock {
         PBF_CUDA(ctx, cudaEventRecord(end, ctx->stream));
         PBF_CUDA(ctx, cudaEventSynchronize(end));
         for (size_t k = 0; k < marks.size(); ++k) {
-            float ms = 0.0f;
-            cudaEvent_t next = k + 1 < marks.size() ? marks[k + 1].second : end;
-            cudaEventElapsedTime(&ms, marks[k].second, next);
-            ctx->stageMs[marks[k].first] += ms;
+            float ms = 0.0f, t0 = 0.0f, t1 = 0.0f;
+            cudaEvent_t next = k + 1 < marks.size() ? marks[k + 1].event : end;
+            cudaEventElapsedTime(&ms, marks[k].event, next);
+            ctx->stageMs[marks[k].stage] += ms;
+            PbfPerfTracker& t = ctx->trackers[marks[k].tracker];
+            if (ctx->timingAnchor) {
+                cudaEventElapsedTime(&t0, ctx->timingAnchor, marks[k].event);
+                cudaEventElapsedTime(&t1, ctx->timingAnchor, next);
+            }
+            t.time_start = (uint64_t)((double)t0 * 1e6);
+            t.time_end = (uint64_t)((double)t1 * 1e6);
+            // OCLPerfMon::UpdateTimings (src/OCLPerfMon.cpp:33-49): weight 0.5
+            t.total_time = (double)ms * (1.0 - 0.5) + t.last_time * 0.5;
+            t.last_time = t.total_time;
         }
-        for (auto& m : marks) cudaEventDestroy(m.second);
+        for (auto& m : marks) cudaEventDestroy(m.event);
         cudaEventDestroy(end);
         marks.clear();
         return PBF_OK;
@@ -357,7 +388,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     const int P = ctx->curPos, V = ctx->curVel;
     const bool paused = ctx->paused != 0;
     uint64_t launched = 0;
-    auto mark = [&](const char* name) { return clock ? clock->stage(name) : PBF_OK; };
+    auto mark = [&](const char* name, int iteration = -1) { return clock ? clock->stage(name, iteration) : PBF_OK; };
 
     mark("predictPositions");
     const pbf::Batch b = batch_of(ctx);
@@ -396,9 +427,9 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     const unsigned iters = ctx->params.simIterations;
     for (unsigned it = 0; it < iters; ++it) {
         float4* packed = tape ? tape->q[it] : ctx->pred[a ^ 1];
-        mark("computeScaling");
+        mark("computeScaling", (int)it);
         pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, ls.scaling, s);
-        mark("computeDelta");
+        mark("computeDelta", (int)it);
         pbf::launch_compute_delta(c, b, packed, ctx->pos[sortedPos], ctx->pred[a], ctx->density, list, meta,
                                   it + 1 == iters, tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr,
                                   ls.delta, s);
@@ -613,6 +644,7 @@ int pbf_destroy(pbf_ctx* ctx) {
     dev_free(ctx->list); dev_free(ctx->meta); dev_free(ctx->errWord);
     dev_free(ctx->scenes); dev_free(ctx->sceneOf); dev_free(ctx->ids); dev_free(ctx->idsTmp);
     dev_free(ctx->quadsDev); dev_free(ctx->maskDev); dev_free(ctx->waveDev);
+    if (ctx->timingAnchor) cudaEventDestroy(ctx->timingAnchor);
     for (auto& k : ctx->ckpt) { dev_free(k.pos); dev_free(k.vel); dev_free(k.ids); }
     dev_free(ctx->ckptEnd.pos); dev_free(ctx->ckptEnd.vel); dev_free(ctx->ckptEnd.ids);
     free_tape(ctx);
@@ -1056,9 +1088,47 @@ int pbf_read_friends(pbf_ctx* ctx, uint32_t* counts, uint32_t* list, int list_sl
 
 int pbf_enable_stage_timing(pbf_ctx* ctx, int enable) {
     if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    const bool was = ctx->stageTiming;
     ctx->stageTiming = enable != 0;
     ctx->stageNames.clear();
     ctx->stageMs.clear();
+    if (ctx->stageTiming && !was) {
+        ctx->trackers.clear();
+        PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+        if (!ctx->timingAnchor) PBF_CUDA(ctx, cudaEventCreate(&ctx->timingAnchor));
+        PBF_CUDA(ctx, cudaEventRecord(ctx->timingAnchor, ctx->stream));
+    }
+    return PBF_OK;
+}
+
+int pbf_perf_trackers(pbf_ctx* ctx, PbfPerfTracker* out, int capacity, int* count) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    const int k = (int)ctx->trackers.size();
+    if (count) *count = k;
+    if (out)
+        for (int i = 0; i < std::min(k, capacity); ++i) out[i] = ctx->trackers[i];
+    return PBF_OK;
+}
+
+int pbf_perf_export_json(pbf_ctx* ctx, char* buf, size_t capacity, size_t* length) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    std::string s = "{\"trackers\": [";
+    double total = 0.0;
+    char line[256];
+    for (size_t i = 0; i < ctx->trackers.size(); ++i) {
+        const PbfPerfTracker& t = ctx->trackers[i];
+        std::snprintf(line, sizeof line,
+                      "%s{\"eventName\": \"%s\", \"time_start\": %llu, \"time_end\": %llu, \"total_time\": %.6f, "
+                      "\"last_time\": %.6f}",
+                      i ? ", " : "", t.eventName, (unsigned long long)t.time_start, (unsigned long long)t.time_end,
+                      t.total_time, t.last_time);
+        s += line;
+        total += t.total_time;
+    }
+    std::snprintf(line, sizeof line, "], \"total_time\": %.6f, \"unit\": \"ms\"}", total);
+    s += line;
+    if (length) *length = s.size() + 1;
+    if (buf && capacity) std::snprintf(buf, capacity, "%s", s.c_str());
     return PBF_OK;
 }
 

@@ -64,6 +64,12 @@ QUAD_DTYPE = np.dtype([("B", "<f4", 3), ("E0", "<f4", 3), ("E1", "<f4", 3), ("ma
                        ("maskHeight", "<i4")])
 
 
+class PbfPerfTracker(ctypes.Structure):
+    """PbfPerfTracker (include/pbf_capi.h): the reference's PM_PERFORMANCE_TRACKER fields."""
+    _fields_ = [("eventName", ctypes.c_char * 48), ("time_start", c_uint64), ("time_end", c_uint64),
+                ("total_time", ctypes.c_double), ("last_time", ctypes.c_double)]
+
+
 class PbfError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"[{code}] {message}")
@@ -119,6 +125,8 @@ def library() -> ctypes.CDLL:
         "pbf_read_ids": [c_void_p, u32p],
         "pbf_set_force_quads": [c_void_p, c_void_p, c_int],
         "pbf_set_wave_position": [c_void_p, c_float],
+        "pbf_perf_trackers": [c_void_p, c_void_p, c_int, POINTER(c_int)],
+        "pbf_perf_export_json": [c_void_p, c_char_p, c_size_t, POINTER(c_size_t)],
         "pbf_save_state": [c_void_p, ctypes.c_char_p],
         "pbf_load_state": [c_void_p, ctypes.c_char_p],
         "pbf_rollout_forward": [c_void_p, c_int, c_int],
@@ -369,6 +377,22 @@ class Simulation:
         q = np.ascontiguousarray(quads, QUAD_DTYPE) if quads is not None else np.zeros(0, QUAD_DTYPE)
         _check(self.lib.pbf_set_force_quads(self._ctx, q.ctypes.data if len(q) else None, len(q)), self._ctx)
 
+    def perf_trackers(self) -> list:
+        """[(eventName, time_start ns, time_end ns, total_time ms, last_time ms)] in order of first use."""
+        count = c_int(0)
+        _check(self.lib.pbf_perf_trackers(self._ctx, None, 0, ctypes.byref(count)), self._ctx)
+        arr = (PbfPerfTracker * max(1, count.value))()
+        _check(self.lib.pbf_perf_trackers(self._ctx, arr, count.value, ctypes.byref(count)), self._ctx)
+        return [(t.eventName.decode(), t.time_start, t.time_end, t.total_time, t.last_time)
+                for t in arr[:count.value]]
+
+    def perf_json(self) -> str:
+        need = c_size_t(0)
+        _check(self.lib.pbf_perf_export_json(self._ctx, None, 0, ctypes.byref(need)), self._ctx)
+        buf = ctypes.create_string_buffer(need.value)
+        _check(self.lib.pbf_perf_export_json(self._ctx, buf, need.value, ctypes.byref(need)), self._ctx)
+        return buf.value.decode()
+
     def set_wave_position(self, wave_pos: float) -> None:
         _check(self.lib.pbf_set_wave_position(self._ctx, float(wave_pos)), self._ctx)
 
@@ -433,6 +457,7 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_create_batch", "pbf_scene_offsets", "pbf_get_launch_shape", "pbf_set_launch_shape", "pbf_autotune",
         "pbf_read_ids", "pbf_rollout_forward", "pbf_rollout_backward", "pbf_set_force_quads",
         "pbf_set_wave_position", "pbf_wave_position", "pbf_save_state", "pbf_load_state",
+        "pbf_perf_trackers", "pbf_perf_export_json",
     ])
 
 

@@ -50,7 +50,7 @@ int main(int argc, char** argv) {
         std::ofstream out(argv[4], std::ios::binary);
         out.write(reinterpret_cast<const char*>(pos.data()), pos.size() * sizeof(float));
         out.write(reinterpret_cast<const char*>(vel.data()), vel.size() * sizeof(float));
-        for (const auto& t : simulation.PerfData) std::cout << t.eventName << " " << t.total_time << "\n";
+        for (const auto* t : simulation.PerfData.Trackers) std::cout << t->eventName << " " << t->total_time << "\n";
     } catch (const std::runtime_error& e) {
         std::cerr << "error: " << e.what() << "\n";
         return 3;

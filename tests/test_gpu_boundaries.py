@@ -62,3 +62,30 @@ def test_state_file_round_trip(pbf_mod, cuda_device, tmp_path):
         (tmp_path / "junk").write_bytes(b"not a state file")
         with pytest.raises(pbf_mod.PbfError):
             c.load_state(tmp_path / "junk")
+
+
+def test_perf_trackers_follow_the_reference_monitor(pbf_mod, cuda_device):
+    """Trackers named as OCLPerfMon names them, smoothed with weight 0.5
+    (src/OCLPerfMon.cpp:33-49), exported as JSON for dashboards."""
+    import json
+    params, pos, vel = pbf_mod.make_scene("dam_break_32k")
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        sim.enable_stage_timing(True)
+        sim.Step(1)
+        first = {t[0]: t for t in sim.perf_trackers()}
+        sim.Step(1)
+        second = sim.perf_trackers()
+        doc = json.loads(sim.perf_json())
+    iters = int(params.simIterations)
+    names = [t[0] for t in second]
+    want = (["predictPositions", "radixsort", "sortParticles", "updateCells", "buildFriendsList", "resetPartList"] +
+            [x for i in range(iters) for x in (f"computeScaling_{i}", f"computeDelta_{i}")] +
+            ["updateVelocities", "applyViscosity", "applyVorticity"])
+    assert names == want
+    for name, start, end, total, last in second:
+        assert end >= start and total > 0 and total == last
+        assert end > first[name][2]                     # timestamps advance
+        # total = 0.5 * current + 0.5 * previous, with current >= 0
+        assert total >= 0.5 * first[name][3] - 1e-9
+    assert [t["eventName"] for t in doc["trackers"]] == want
+    assert abs(doc["total_time"] - sum(t[3] for t in second)) < 1e-3
