@@ -323,6 +323,39 @@ int pbf_rollout_forward(pbf_ctx* ctx, int substeps, int checkpoint_every);
    state is left at the end of the rollout. */
 int pbf_rollout_backward(pbf_ctx* ctx, const float* dL_dx, float* dL_dv0, float* dL_dvisc, float* dL_dg);
 
+/* ------------------------------------------------------ headless render -- */
+
+/* PbfCamera (include/pbf_params.h) is the renderer's camera. */
+
+/* Fill *cam like the reference: lookAt(eye, at, up), perspective(fovyDeg,
+   width/height, 0.1, 1000), widthOfNearPlane = width / (2 tan(fovy/2)),
+   invFocalLen = (tan(fovy/2) aspect, tan(fovy/2)). */
+int pbf_render_camera(const float eye[3], const float at[3], const float up[3], float fovyDeg, int width, int height,
+                      float pointSize, PbfCamera* cam);
+
+/* Render the current particle positions into width x height RGBA float
+   images on the device (no graphics API; the shaders' arithmetic as CUDA
+   kernels, pixel (0,0) at the bottom left as in OpenGL windows):
+     mode 0 (smooth, UICmd_RenderMode 0): particles.vs + particles_color.fs
+       splat the particles as sphere impostors with a LEQUAL depth test
+       (colour = fragment depth, particle index), then vis_scan.cms marks the
+       visible particles, grid_build.cms hashes them into a 2048 x 2048 grid,
+       fluid_depth_smoothing.fs moves every pixel onto the density shell
+       (colour = depth, gradient direction) and fluid_final_render.fs shades
+       it;
+     mode 1 / 2: the splat coloured by speed / by particle index
+       (particles_color.fs renderMethod 1 / 2), copied to the output.
+   Orders the shaders leave to the hardware are fixed: among fragments of
+   equal depth the last drawn (highest index) wins, and a grid cell's chain
+   lists its visible particles in decreasing index order.  Reproducible bit
+   for bit against the oracle's restatement. */
+int pbf_render_frame(pbf_ctx* ctx, const PbfCamera* cam, int mode);
+
+/* Copy an image of the last pbf_render_frame to host memory (width x height
+   float4, row 0 at the bottom): which 0 = output, 1 = splat colour,
+   2 = smoothed depth (mode 0 only). */
+int pbf_render_read(pbf_ctx* ctx, int which, float* rgba);
+
 /* ------------------------------------------------------------ autotuner -- */
 
 /* Threads per block of the five neighbour kernels, in the order friends,

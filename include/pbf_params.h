@@ -90,6 +90,21 @@ typedef struct PbfForceQuad {
     int32_t maskYOffset, maskHeight;
 } PbfForceQuad;
 
+/* The camera of the reference's particle renderer (src/visual/visual.cpp:108-127,
+   src/ZPR.cpp:32-37), as data.  Matrices are column-major, as glm hands them
+   to OpenGL.  depthRange is the (near, far) that fluid_depth_smoothing.fs and
+   fluid_final_render.fs linearise depth with (0.1, 1000 in the reference). */
+typedef struct PbfCamera {
+    float modelView[16];
+    float invModelView[16];
+    float projection[16];
+    float invFocalLen[2];
+    float depthRange[2];
+    float widthOfNearPlane;
+    float pointSize;         /* Params.particleRenderSize */
+    int32_t width, height;   /* pixels, each at most 8192 */
+} PbfCamera;
+
 /* Largest number of force planes. */
 #define PBF_MAX_FORCE_QUADS        64
 

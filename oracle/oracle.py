@@ -56,6 +56,8 @@ def lib() -> ctypes.CDLL:
         l.oracle_set_force_planes.restype = c_int
         l.oracle_set_wave_position.argtypes = [c_float]
         l.oracle_set_wave_position.restype = None
+        l.oracle_render.argtypes = [c_void_p, c_int, c_int, c_float, c_void_p, c_void_p, c_void_p, c_void_p]
+        l.oracle_render.restype = c_int
         l.oracle_noise_sinf.argtypes = [c_float]
         l.oracle_noise_sinf.restype = c_float
         _lib = l
@@ -108,6 +110,20 @@ def ref_set_force_mask(mask=None):
 def set_wave_position(wave_pos: float = 0.0) -> None:
     """The moving wall (xMin + wave_pos) of every later oracle step."""
     lib().oracle_set_wave_position(float(wave_pos))
+
+
+def render(cam, mode, params, pos):
+    """The renderer's restatement: (splat, smooth, out) as [height, width, 4]
+    float32 images (smooth is None outside mode 0).  cam: a ctypes PbfCamera."""
+    n = int(params.particleCount)
+    p = np.ascontiguousarray(pos, np.float32).reshape(n, 4)
+    shape = (cam.height, cam.width, 4)
+    splat, out = np.zeros(shape, np.float32), np.zeros(shape, np.float32)
+    smooth = np.zeros(shape, np.float32) if mode == 0 else None
+    rc = lib().oracle_render(ctypes.byref(cam), mode, n, float(params.h), _ptr(p), _ptr(splat), _ptr(smooth), _ptr(out))
+    if rc != 0:
+        raise ValueError("oracle_render rejected the arguments")
+    return splat, smooth, out
 
 
 def noise_sinf(x: float) -> float:

@@ -1257,6 +1257,244 @@ int oracle_set_force_planes(const PbfForceQuad* quads, int count, const uint32_t
 // x bound is xMin + wavePos.
 void oracle_set_wave_position(float wavePos) { g_wave = wavePos; }
 
+// ---- headless render: the reference's particle shaders restated ----
+// particles.vs + particles_color.fs (splat), vis_scan.cms, grid_build.cms,
+// fluid_depth_smoothing.fs, fluid_final_render.fs; the orders the shaders
+// leave to the hardware fixed as the library fixes them (equal depths: the
+// last drawn wins; a bucket's chain in decreasing particle index).
+namespace render {
+struct V4 { float x, y, z, w; };
+static V4 mat_mul(const float* m, float x, float y, float z, float w) {
+    return {((m[0] * x + m[4] * y) + m[8] * z) + m[12] * w, ((m[1] * x + m[5] * y) + m[9] * z) + m[13] * w,
+            ((m[2] * x + m[6] * y) + m[10] * z) + m[14] * w, ((m[3] * x + m[7] * y) + m[11] * z) + m[15] * w};
+}
+static float dot3(float ax, float ay, float az, float bx, float by, float bz) { return (ax * bx + ay * by) + az * bz; }
+static float gmax(float x, float y) { return x < y ? y : x; }
+static float gmin(float x, float y) { return y < x ? y : x; }
+static float gclamp(float x, float a, float b) { return gmin(gmax(x, a), b); }
+static int to_int(float v) {  // truncation, saturating, NaN -> 0
+    if (v != v) return 0;
+    if (v >= 2147483648.0f) return 2147483647;
+    if (v <= -2147483648.0f) return (-2147483647 - 1);
+    return (int)v;
+}
+static uint32_t expand(int xi) {
+    uint32_t x = (uint32_t)xi;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+static const uint32_t kBuckets = 2048u * 2048u;
+static uint32_t bucket(int x, int y, int z) {
+    const int m = (int)(expand(x) | (expand(y) << 1) | (expand(z) << 2));
+    return (uint32_t)(m % (int)kBuckets);
+}
+struct Sprite { float ex, ey, ez, xw, yw, s; };
+static bool sprite(const PbfCamera& cam, const float* p, Sprite& sp) {
+    const V4 e = mat_mul(cam.modelView, p[0], p[1], p[2], 1.0f);
+    const V4 c = mat_mul(cam.projection, e.x, e.y, e.z, e.w);
+    if (!(c.w > 0.0f)) return false;
+    const float nx = c.x / c.w, ny = c.y / c.w, nz = c.z / c.w;
+    if (!(std::fabs(nx) <= 1.0f && std::fabs(ny) <= 1.0f && std::fabs(nz) <= 1.0f)) return false;
+    float s = cam.widthOfNearPlane * cam.pointSize / c.w;
+    s = std::fmin(std::fmax(s, 1.0f), 1024.0f);
+    const float hw = 0.5f * (float)cam.width, hh = 0.5f * (float)cam.height;
+    sp = {e.x, e.y, e.z, nx * hw + hw, ny * hh + hh, s};
+    return true;
+}
+struct Frag { float nx, ny, nz, depth; };
+static bool fragment(const PbfCamera& cam, const Sprite& sp, int i, int j, Frag& f) {
+    const float pcx = 0.5f + (((float)i + 0.5f) - sp.xw) / sp.s;
+    const float pcy = 0.5f - (((float)j + 0.5f) - sp.yw) / sp.s;
+    f.nx = pcx * 2.0f + -1.0f;
+    f.ny = pcy * 2.0f + -1.0f;
+    const float mag = f.nx * f.nx + f.ny * f.ny;
+    if (mag > 1.0f) return false;
+    f.nz = std::sqrt(1.0f - mag);
+    const V4 c = mat_mul(cam.projection, sp.ex + f.nx * cam.pointSize, sp.ey + f.ny * cam.pointSize,
+                         sp.ez + f.nz * cam.pointSize, 1.0f);
+    const float ndc = c.z / c.w;
+    if (ndc < -1.0f) return false;
+    f.depth = ((1.0f * ndc + 0.0f) + 1.0f) / 2.0f;
+    return f.depth <= 1.0f;
+}
+static float hsv_channel(float h, float k, float s, float v) {
+    const float x = h + k;
+    const float fr = x - std::floor(x);
+    const float p = std::fabs(fr * 6.0f - 3.0f);
+    const float q = gclamp(p - 1.0f, 0.0f, 1.0f);
+    return v * (1.0f * (1.0f - s) + q * s);
+}
+static V4 pixel_world(const PbfCamera& cam, int i, int j, float z) {
+    const float nearv = cam.depthRange[0], farv = cam.depthRange[1];
+    const float lz = nearv / (farv - z * (farv - nearv)) * farv;
+    const float u = (((float)i + 0.5f) / (float)cam.width * 2.0f - 1.0f) * cam.invFocalLen[0];
+    const float v = (((float)j + 0.5f) / (float)cam.height * 2.0f - 1.0f) * cam.invFocalLen[1];
+    return mat_mul(cam.invModelView, u * lz, v * lz, -lz, 1.0f);
+}
+static void normalize3(float& x, float& y, float& z) {
+    const float l = std::sqrt(dot3(x, y, z, x, y, z));
+    x = x / l; y = y / l; z = z / l;
+}
+static float pow50(float x) {
+    if (!(x >= 0.0f)) return std::nanf("");
+    const float x2 = x * x, x4 = x2 * x2, x8 = x4 * x4, x16 = x8 * x8, x32 = x16 * x16;
+    return (x32 * x16) * x2;
+}
+}  // namespace render
+
+// The frame of pbf_render_frame: splat, smooth (mode 0 only) and out
+// receive width x height float4 images (row 0 at the bottom); any may be NULL.
+int oracle_render(const PbfCamera* camp, int mode, int n, float h, const float* pos, float* splat, float* smooth,
+                  float* out) {
+    using namespace render;
+    if (!camp || n < 1 || !pos || mode < 0 || mode > 2) return -1;
+    const PbfCamera& cam = *camp;
+    const int W = cam.width, H = cam.height;
+    const size_t pixels = (size_t)W * H;
+    std::vector<float> depth(pixels, 2.0f);
+    std::vector<int64_t> winner(pixels, -1);
+    for (int p = 0; p < n; ++p) {  // draw order
+        Sprite sp;
+        if (!sprite(cam, pos + 4 * (size_t)p, sp)) continue;
+        const int i0 = std::max(0, (int)std::ceil(sp.xw - sp.s * 0.5f - 0.5f));
+        const int i1 = std::min(W - 1, (int)std::ceil(sp.xw + sp.s * 0.5f - 0.5f) - 1);
+        const int j0 = std::max(0, (int)std::ceil(sp.yw - sp.s * 0.5f - 0.5f));
+        const int j1 = std::min(H - 1, (int)std::ceil(sp.yw + sp.s * 0.5f - 0.5f) - 1);
+        for (int j = j0; j <= j1; ++j)
+            for (int i = i0; i <= i1; ++i) {
+                Frag f;
+                if (!fragment(cam, sp, i, j, f)) continue;
+                const size_t k = (size_t)j * W + i;
+                if (f.depth <= depth[k]) { depth[k] = f.depth; winner[k] = p; }  // LEQUAL
+            }
+    }
+    std::vector<float> sc(4 * pixels, 0.0f);
+    for (size_t k = 0; k < pixels; ++k) {
+        if (winner[k] < 0) continue;
+        const int p = (int)winner[k], i = (int)(k % W), j = (int)(k / W);
+        float* c = &sc[4 * k];
+        if (mode == 0) { c[0] = depth[k]; c[1] = (float)p; c[2] = 0.0f; c[3] = 1.0f; continue; }
+        Sprite sp;
+        Frag f{};
+        sprite(cam, pos + 4 * (size_t)p, sp);
+        fragment(cam, sp, i, j, f);
+        const float cosA = gclamp(dot3(f.nx, f.ny, f.nz, 1.0f, 1.0f, 1.0f), 0.0f, 1.0f);
+        float r, g, b;
+        if (mode == 1) {
+            const float v = pos[4 * (size_t)p + 3] / 20.0f;
+            r = v; g = v; b = 1.0f;
+        } else {
+            const float hue = (float)p / (float)n * 0.7f;
+            r = hsv_channel(hue, 1.0f, 0.9f, 0.9f);
+            g = hsv_channel(hue, 2.0f / 3.0f, 0.9f, 0.9f);
+            b = hsv_channel(hue, 1.0f / 3.0f, 0.9f, 0.9f);
+        }
+        c[0] = r * cosA; c[1] = g * cosA; c[2] = b * cosA; c[3] = 1.0f * cosA;
+    }
+    if (splat) std::memcpy(splat, sc.data(), 16 * pixels);
+    if (mode != 0) {
+        if (out) std::memcpy(out, sc.data(), 16 * pixels);
+        return 0;
+    }
+    // visible particles and their buckets
+    std::vector<uint8_t> vis((size_t)n, 0);
+    for (size_t k = 0; k < pixels; ++k) {
+        const uint32_t x = (uint32_t)(sc[4 * k + 1] + 0.5f);
+        if (x < (uint32_t)n) vis[x] = 1;
+    }
+    std::vector<std::vector<int>> chains;
+    std::vector<int32_t> slot(kBuckets, -1);
+    for (int p = 0; p < n; ++p) {
+        if (!vis[p]) continue;
+        const float* q = pos + 4 * (size_t)p;
+        const uint32_t b = bucket(to_int(q[0] / h), to_int(q[1] / h), to_int(q[2] / h));
+        if (slot[b] < 0) { slot[b] = (int32_t)chains.size(); chains.emplace_back(); }
+        chains[slot[b]].push_back(p);
+    }
+    auto sample = [&](float wx, float wy, float wz, float& density, float& gx, float& gy, float& gz) {
+        const float h2 = h * h;
+        density = 0.0f; gx = gy = gz = 0.0f;
+        const int cx = to_int(wx / h), cy = to_int(wy / h), cz = to_int(wz / h);
+        for (int iz = -1; iz <= 1; ++iz)
+            for (int iy = -1; iy <= 1; ++iy)
+                for (int ix = -1; ix <= 1; ++ix) {
+                    const int32_t sl = slot[bucket(cx + ix, cy + iy, cz + iz)];
+                    if (sl < 0) continue;
+                    const std::vector<int>& ch = chains[sl];
+                    for (size_t t = ch.size(); t-- > 0;) {
+                        const float* pp = pos + 4 * (size_t)ch[t];
+                        const float dx = pp[0] - wx, dy = pp[1] - wy, dz = pp[2] - wz;
+                        const float r2 = dot3(dx, dy, dz, dx, dy, dz);
+                        if (r2 < h2) {
+                            const float d = h2 - r2;
+                            gx = gx + dx * d * d;
+                            gy = gy + dy * d * d;
+                            gz = gz + dz * d * d;
+                            density = density + d * d * d;
+                        }
+                    }
+                }
+        density = density * 1.0f;
+        gx = gx * -6.0f; gy = gy * -6.0f; gz = gz * -6.0f;
+    };
+    std::vector<float> sm(4 * pixels, 0.0f);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long long kk = 0; kk < (long long)pixels; ++kk) {
+        const size_t k = (size_t)kk;
+        const int i = (int)(k % W), j = (int)(k / W);
+        const float z = sc[4 * k];
+        if (z == 1.0f) continue;
+        const render::V4 m = pixel_world(cam, i, j, z);
+        float nx = cam.invModelView[12] - m.x, ny = cam.invModelView[13] - m.y, nz = cam.invModelView[14] - m.z;
+        normalize3(nx, ny, nz);
+        float tp = 0.0f, sx = m.x, sy = m.y, sz = m.z, density, gx = 0.0f, gy = 0.0f, gz = 0.0f;
+        for (int it = 0; it < 2; ++it) {
+            sample(sx, sy, sz, density, gx, gy, gz);
+            const float dd = density - 1.0f;
+            const float ga = dot3(nx, ny, nz, gx, gy, gz);
+            tp += dd / ga;
+            sx = m.x + tp * nx; sy = m.y + tp * ny; sz = m.z + tp * nz;
+        }
+        const render::V4 vs = mat_mul(cam.modelView, sx, sy, sz, 1.0f);
+        const render::V4 c = mat_mul(cam.projection, vs.x, vs.y, vs.z, 1.0f);
+        const float ndc = c.z / c.w;
+        if (ndc < -1.0f) continue;
+        normalize3(gx, gy, gz);
+        float* r = &sm[4 * k];
+        r[0] = ((1.0f * ndc + 0.0f) + 1.0f) / 2.0f; r[1] = gx; r[2] = gy; r[3] = gz;
+    }
+    if (smooth) std::memcpy(smooth, sm.data(), 16 * pixels);
+    if (!out) return 0;
+    std::vector<float> fo(4 * pixels, 0.0f);
+    const int di[5] = {0, 1, -1, 0, 0}, dj[5] = {0, 0, 0, 1, -1};
+    for (size_t k = 0; k < pixels; ++k) {
+        const int i = (int)(k % W), j = (int)(k / W);
+        bool discard = false;
+        for (int q = 0; q < 5 && !discard; ++q) {
+            const int a = i + di[q], b = j + dj[q];
+            const float z = (a >= 0 && a < W && b >= 0 && b < H) ? sm[4 * ((size_t)b * W + a)] : 0.0f;
+            discard = (z == 1.0f);
+        }
+        if (discard) continue;
+        const float* s = &sm[4 * k];
+        const render::V4 w = pixel_world(cam, i, j, s[0]);
+        float ex = cam.invModelView[12] - w.x, ey = cam.invModelView[13] - w.y, ez = cam.invModelView[14] - w.z;
+        normalize3(ex, ey, ez);
+        const float lx = 0.0f, ly = 1.0f, lz = 0.0f;
+        float hx = lx + ex, hy = ly + ey, hz = lz + ez;
+        normalize3(hx, hy, hz);
+        const float diff = gclamp(dot3(lx, ly, lz, s[1], s[2], s[3]), 0.0f, 1.0f);
+        const float spec = gmax(0.0f, pow50(dot3(s[1], s[2], s[3], hx, hy, hz)));
+        float* r = &fo[4 * k];
+        r[0] = 0.0f * diff + 1.0f * spec; r[1] = 0.0f * diff + 1.0f * spec; r[2] = 0.5f * diff + 1.0f * spec; r[3] = 1.0f;
+    }
+    std::memcpy(out, fo.data(), 16 * pixels);
+    return 0;
+}
+
 // The force planes' noise sine, for the tests.
 float oracle_noise_sinf(float x) { return noise_sinf_ref(x); }
 

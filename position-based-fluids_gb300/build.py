@@ -36,6 +36,7 @@ CUDA_UNITS = {
     "pbf_capi.cu": ["--fmad=false"],
     "pbf_noalloc.cu": ["--fmad=false"],
     "pbf_adjoint.cu": [],
+    "pbf_render.cu": ["--fmad=false"],
 }
 CXX_UNITS = ["params.cpp"]
 

@@ -59,6 +59,8 @@ struct pbf_ctx {
     std::vector<uint32_t> sceneOffsets;
     pbf::SceneParams* scenes = nullptr;      // device table, batches only
     float* waveDev = nullptr;                // moving wall offset (pbf_set_wave_position)
+    pbf::RenderBuffers render;               // pbf_render_frame
+    int renderMode = -1;
     pbf::QuadDev* quadsDev = nullptr;        // force planes (pbf_set_force_quads)
     int nquads = 0;
     uint32_t* maskDev = nullptr;             // force mask (pbf_load_force_masks)
@@ -254,6 +256,14 @@ pbf::QuadDev quad_constants(const PbfForceQuad& in) {
 }
 
 void drop_graph(pbf_ctx* ctx);
+
+void free_render(pbf_ctx* ctx) {
+    pbf::RenderBuffers& r = ctx->render;
+    dev_free(r.dkey); dev_free(r.splat); dev_free(r.smooth); dev_free(r.out); dev_free(r.vis);
+    for (int k = 0; k < 2; ++k) { dev_free(r.keys[k]); dev_free(r.perm[k]); }
+    dev_free(r.hist); dev_free(r.cells);
+    r.width = r.height = r.n = 0;
+}
 
 // Copies the force planes and mask into the kernel constants.
 void apply_planes(pbf_ctx* ctx) {
@@ -645,6 +655,7 @@ int pbf_destroy(pbf_ctx* ctx) {
     dev_free(ctx->scenes); dev_free(ctx->sceneOf); dev_free(ctx->ids); dev_free(ctx->idsTmp);
     dev_free(ctx->quadsDev); dev_free(ctx->maskDev); dev_free(ctx->waveDev);
     if (ctx->timingAnchor) cudaEventDestroy(ctx->timingAnchor);
+    free_render(ctx);
     for (auto& k : ctx->ckpt) { dev_free(k.pos); dev_free(k.vel); dev_free(k.ids); }
     dev_free(ctx->ckptEnd.pos); dev_free(ctx->ckptEnd.vel); dev_free(ctx->ckptEnd.ids);
     free_tape(ctx);
@@ -842,6 +853,101 @@ int pbf_load_state(pbf_ctx* ctx, const char* path) {
     PBF_CUDA(ctx, cudaMemcpyAsync(ctx->pos[ctx->curPos], pos.data(), 16 * n, cudaMemcpyHostToDevice, ctx->stream));
     PBF_CUDA(ctx, cudaMemcpyAsync(ctx->vel[ctx->curVel], vel.data(), 16 * n, cudaMemcpyHostToDevice, ctx->stream));
     PBF_CUDA(ctx, cudaMemcpyAsync(ctx->ids, ids.data(), 4 * n, cudaMemcpyHostToDevice, ctx->stream));
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PBF_OK;
+}
+
+int pbf_render_camera(const float eye[3], const float at[3], const float up[3], float fovyDeg, int width, int height,
+                      float pointSize, PbfCamera* cam) {
+    if (!eye || !at || !up || !cam || width < 1 || height < 1 || !(fovyDeg > 0.0f && fovyDeg < 180.0f))
+        return fail(nullptr, PBF_ERR_INVALID, "pbf_render_camera: bad arguments");
+    const double PI = 3.14159265358979323846;
+    double f[3] = {(double)at[0] - eye[0], (double)at[1] - eye[1], (double)at[2] - eye[2]};
+    auto norm = [](double* v) {
+        const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        for (int k = 0; k < 3; ++k) v[k] /= l;
+    };
+    auto cross = [](const double* a, const double* b, double* o) {
+        o[0] = a[1] * b[2] - a[2] * b[1]; o[1] = a[2] * b[0] - a[0] * b[2]; o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    norm(f);
+    const double upd[3] = {up[0], up[1], up[2]};
+    double s[3], v[3];
+    cross(f, upd, s);
+    norm(s);
+    cross(s, f, v);
+    const double e[3] = {eye[0], eye[1], eye[2]};
+    auto dot = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    // glm::lookAt, column-major m[col * 4 + row]
+    double mv[16] = {s[0], v[0], -f[0], 0, s[1], v[1], -f[1], 0, s[2], v[2], -f[2], 0, -dot(s, e), -dot(v, e), dot(f, e), 1};
+    // inverse of the rigid transform: rotation transposed, then the eye
+    double imv[16] = {s[0], s[1], s[2], 0, v[0], v[1], v[2], 0, -f[0], -f[1], -f[2], 0, e[0], e[1], e[2], 1};
+    const double aspect = (double)width / (double)height, zn = 0.1, zf = 1000.0;
+    const double th = std::tan(fovyDeg * PI / 180.0 / 2.0);
+    double pr[16] = {0};
+    pr[0] = 1.0 / (aspect * th);
+    pr[5] = 1.0 / th;
+    pr[10] = -(zf + zn) / (zf - zn);
+    pr[11] = -1.0;
+    pr[14] = -(2.0 * zf * zn) / (zf - zn);
+    for (int k = 0; k < 16; ++k) {
+        cam->modelView[k] = (float)mv[k];
+        cam->invModelView[k] = (float)imv[k];
+        cam->projection[k] = (float)pr[k];
+    }
+    cam->invFocalLen[0] = (float)(th * aspect);
+    cam->invFocalLen[1] = (float)th;
+    cam->depthRange[0] = 0.1f;
+    cam->depthRange[1] = 1000.0f;
+    cam->widthOfNearPlane = (float)(width / (2.0 * std::tan(0.5 * fovyDeg * PI / 180.0)));
+    cam->pointSize = pointSize;
+    cam->width = width;
+    cam->height = height;
+    return PBF_OK;
+}
+
+int pbf_render_frame(pbf_ctx* ctx, const PbfCamera* cam, int mode) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!cam || cam->width < 1 || cam->height < 1 || cam->width > 8192 || cam->height > 8192 || mode < 0 || mode > 2)
+        return fail(ctx, PBF_ERR_INVALID, "pbf_render_frame: camera size must be 1..8192 and mode 0..2");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    pbf::RenderBuffers& r = ctx->render;
+    const size_t pixels = (size_t)cam->width * cam->height;
+    if (r.width != cam->width || r.height != cam->height || r.n != ctx->n) {
+        free_render(ctx);
+        const size_t n = (size_t)ctx->n;
+        r.plan = pbf::make_sort_plan(ctx->n, 1u << 23);
+        if ((rc = dev_alloc(ctx, &r.dkey, pixels)) || (rc = dev_alloc(ctx, &r.splat, pixels)) ||
+            (rc = dev_alloc(ctx, &r.smooth, pixels)) || (rc = dev_alloc(ctx, &r.out, pixels)) ||
+            (rc = dev_alloc(ctx, &r.vis, n)) || (rc = dev_alloc(ctx, &r.keys[0], n)) ||
+            (rc = dev_alloc(ctx, &r.keys[1], n)) || (rc = dev_alloc(ctx, &r.perm[0], n)) ||
+            (rc = dev_alloc(ctx, &r.perm[1], n)) || (rc = dev_alloc(ctx, &r.hist, r.plan.histWords)) ||
+            (rc = dev_alloc(ctx, &r.cells, pbf::render_grid_words()))) {
+            free_render(ctx);
+            return rc;
+        }
+        r.width = cam->width;
+        r.height = cam->height;
+        r.n = ctx->n;
+    }
+    pbf::render_frame(*cam, mode, ctx->n, ctx->params.h, ctx->pos[ctx->curPos], r, ctx->stream);
+    ctx->launches += pbf::render_launches(mode, r.plan);
+    ctx->renderMode = mode;
+    PBF_CUDA(ctx, cudaGetLastError());
+    PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PBF_OK;
+}
+
+int pbf_render_read(pbf_ctx* ctx, int which, float* rgba) {
+    if (!ctx || !rgba) return fail(ctx, PBF_ERR_INVALID, "pbf_render_read: NULL argument");
+    if (ctx->renderMode < 0) return fail(ctx, PBF_ERR_STATE, "pbf_render_frame has not run");
+    const pbf::RenderBuffers& r = ctx->render;
+    const float4* src = which == 0 ? r.out : which == 1 ? r.splat : which == 2 ? r.smooth : nullptr;
+    if (!src || (which == 2 && ctx->renderMode != 0))
+        return fail(ctx, PBF_ERR_INVALID, "pbf_render_read: which is 0, 1, or 2 after a mode 0 frame");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    PBF_CUDA(ctx, cudaMemcpyAsync(rgba, src, 16 * (size_t)r.width * r.height, cudaMemcpyDeviceToHost, ctx->stream));
     PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return PBF_OK;
 }

@@ -142,4 +142,22 @@ int adjoint_launches(int iterations);
 void scatter_by_id(int n, const uint32_t* ids, const float4* byId, float4* out, cudaStream_t s);
 void gather_to_id(int n, const uint32_t* ids, const float4* in, float4* byId, cudaStream_t s);
 
+// ---- headless render (pbf_render.cu) ----
+struct RenderBuffers {
+    int width = 0, height = 0, n = 0;
+    unsigned long long* dkey = nullptr;  // per pixel: (depth bits, ~particle index) of the nearest fragment
+    float4* splat = nullptr;             // particles_color.fs output
+    float4* smooth = nullptr;            // fluid_depth_smoothing.fs output
+    float4* out = nullptr;               // the frame
+    uint8_t* vis = nullptr;              // per particle: seen in the splat
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* perm[2] = {nullptr, nullptr};
+    uint32_t* hist = nullptr;
+    uint32_t* cells = nullptr;           // 2 x 2048^2: first / last sorted index per bucket
+    SortPlan plan{};
+};
+void render_frame(const PbfCamera& cam, int mode, int n, float h, const float4* pos, RenderBuffers& rb, cudaStream_t s);
+int render_launches(int mode, const SortPlan& plan);
+size_t render_grid_words();
+
 }  // namespace pbf

@@ -64,6 +64,23 @@ QUAD_DTYPE = np.dtype([("B", "<f4", 3), ("E0", "<f4", 3), ("E1", "<f4", 3), ("ma
                        ("maskHeight", "<i4")])
 
 
+class PbfCamera(ctypes.Structure):
+    """PbfCamera (include/pbf_params.h): the renderer's camera, column-major matrices."""
+    _fields_ = [("modelView", c_float * 16), ("invModelView", c_float * 16), ("projection", c_float * 16),
+                ("invFocalLen", c_float * 2), ("depthRange", c_float * 2), ("widthOfNearPlane", c_float),
+                ("pointSize", c_float), ("width", ctypes.c_int32), ("height", ctypes.c_int32)]
+
+
+def render_camera(eye, at, up=(0.0, 1.0, 0.0), fovy_deg: float = 45.0, width: int = 640, height: int = 480,
+                  point_size: float = 1.0) -> PbfCamera:
+    """The reference's camera (lookAt + perspective, src/visual/visual.cpp:108-127)."""
+    cam = PbfCamera()
+    f3 = c_float * 3
+    _check(library().pbf_render_camera(f3(*eye), f3(*at), f3(*up), float(fovy_deg), int(width), int(height),
+                                       float(point_size), ctypes.byref(cam)))
+    return cam
+
+
 class PbfPerfTracker(ctypes.Structure):
     """PbfPerfTracker (include/pbf_capi.h): the reference's PM_PERFORMANCE_TRACKER fields."""
     _fields_ = [("eventName", ctypes.c_char * 48), ("time_start", c_uint64), ("time_end", c_uint64),
@@ -126,6 +143,9 @@ def library() -> ctypes.CDLL:
         "pbf_set_force_quads": [c_void_p, c_void_p, c_int],
         "pbf_set_wave_position": [c_void_p, c_float],
         "pbf_perf_trackers": [c_void_p, c_void_p, c_int, POINTER(c_int)],
+        "pbf_render_camera": [c_void_p, c_void_p, c_void_p, c_float, c_int, c_int, c_float, c_void_p],
+        "pbf_render_frame": [c_void_p, c_void_p, c_int],
+        "pbf_render_read": [c_void_p, c_int, f32p],
         "pbf_perf_export_json": [c_void_p, c_char_p, c_size_t, POINTER(c_size_t)],
         "pbf_save_state": [c_void_p, ctypes.c_char_p],
         "pbf_load_state": [c_void_p, ctypes.c_char_p],
@@ -377,6 +397,15 @@ class Simulation:
         q = np.ascontiguousarray(quads, QUAD_DTYPE) if quads is not None else np.zeros(0, QUAD_DTYPE)
         _check(self.lib.pbf_set_force_quads(self._ctx, q.ctypes.data if len(q) else None, len(q)), self._ctx)
 
+    def render_frame(self, cam: PbfCamera, mode: int = 0) -> None:
+        _check(self.lib.pbf_render_frame(self._ctx, ctypes.byref(cam), int(mode)), self._ctx)
+
+    def render_read(self, cam: PbfCamera, which: int = 0) -> np.ndarray:
+        """[height, width, 4] float32, row 0 at the bottom: 0 output, 1 splat, 2 smoothed depth."""
+        img = np.empty((cam.height, cam.width, 4), np.float32)
+        _check(self.lib.pbf_render_read(self._ctx, int(which), _f32(img)), self._ctx)
+        return img
+
     def perf_trackers(self) -> list:
         """[(eventName, time_start ns, time_end ns, total_time ms, last_time ms)] in order of first use."""
         count = c_int(0)
@@ -457,7 +486,7 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_create_batch", "pbf_scene_offsets", "pbf_get_launch_shape", "pbf_set_launch_shape", "pbf_autotune",
         "pbf_read_ids", "pbf_rollout_forward", "pbf_rollout_backward", "pbf_set_force_quads",
         "pbf_set_wave_position", "pbf_wave_position", "pbf_save_state", "pbf_load_state",
-        "pbf_perf_trackers", "pbf_perf_export_json",
+        "pbf_perf_trackers", "pbf_perf_export_json", "pbf_render_camera", "pbf_render_frame", "pbf_render_read",
     ])
 
 

@@ -188,3 +188,25 @@ def test_noise_sine_accuracy(oracle_mod):
     print(f"noise sine: max error {err.max():.2f} ulp, mean {err.mean():.3f}")
     assert err.max() <= 4.0
     assert oracle_mod.noise_sinf(0.0) == 0.0 and np.isnan(oracle_mod.noise_sinf(float("nan")))
+
+
+def test_render_restatement_sanity(pbf_mod, oracle_mod):
+    """The renderer's restatement on the reference's scene scale: the splat
+    covers the block with window depths in [0, 1]; on covered pixels the
+    smoothing pass lands near the splat depth; colour modes stay in range."""
+    params = pbf_mod.load_scenario("dam_break_32k")
+    params.h, params.h_2 = 2.0, 4.0
+    pos = pbf_mod.scene_block(16, 16, 16, 0.55, (0.3, 0.3, 0.3), 0.05, 7)
+    params.particleCount = len(pos)
+    cam = pbf_mod.render_camera((4.4, 8.0, 30.0), (4.4, 4.0, 4.4), (0.0, 1.0, 0.0), 45.0, 96, 72, 1.0)
+    splat, smooth, out = oracle_mod.render(cam, 0, params, pos)
+    covered = splat[..., 1] > 0
+    assert 0.05 < covered.mean() < 0.9
+    d = splat[covered][:, 0]
+    assert np.all((d > 0.0) & (d <= 1.0))
+    ok = covered & np.isfinite(smooth[..., 0]) & (smooth[..., 0] > 0)
+    assert ok.mean() > 0.5 * covered.mean()
+    assert np.all(np.abs(smooth[ok][:, 0] - splat[ok][:, 0]) < 0.01)
+    for mode in (1, 2):
+        s, _, o = oracle_mod.render(cam, mode, params, pos)
+        assert np.array_equal(s, o) and np.all((o >= 0.0) & (o <= 2.0))
