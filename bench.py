@@ -292,6 +292,8 @@ def gpu_arm(args) -> None:
     sim.set_params(p2)
     for _ in range(3):
         sim.step_async(sub)
+    sim.synchronize()
+    other_blocks = sim.autotune(trial_substeps=2) if not args.no_autotune else sim.launch_shape()
     barrier()
     o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     o0.record(stream)
@@ -300,8 +302,11 @@ def gpu_arm(args) -> None:
     o1.record(stream)
     o1.synchronize()
     other_ms = o0.elapsed_time(o1) / args.steps
-    other_line = {"mode": other, "value": n * iters * sub / (other_ms / 1000.0), "ms_per_step": other_ms}
+    other_line = {"mode": other, "value": n * iters * sub / (other_ms / 1000.0), "ms_per_step": other_ms,
+                  "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm",
+                                      "balance"], other_blocks))}
     sim.set_params(params)
+    sim.set_launch_shape(blocks)
 
     frame_ms = ms / args.steps
     bytes_sub = (444.0 + 56.0 * iters) * n  # whole-substep compulsory bytes, P = 3 sort passes
@@ -325,7 +330,7 @@ def gpu_arm(args) -> None:
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "working set larger than L2 (no flush)", "mode": MODES[args.math],
                    "cuda_graph": True,
-                   "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity"], blocks))},
+                   "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm", "balance"], blocks))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
                 "steps": e2e_steps},
         "gpu_launches": int(launches),
@@ -466,7 +471,7 @@ def batched(args) -> None:
     single.close()
     line = {"batched": f"{len(scenes)} dam-break scenes", "particles": total, "value": batch_rate, "unit": UNIT,
             "ms_per_step": batch_ms, "steps": args.steps, "warmup": args.warmup, "gpu_launches": int(launches),
-            "autotuned_blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity"], blocks)),
+            "autotuned_blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm", "balance"], blocks)),
             "sequential_value": seq_rate, "ratio_vs_sequential": batch_rate / seq_rate,
             "single_scene_value": single_rate, "ratio_vs_single_scene": batch_rate / single_rate,
             "config": {"scenes": len(scenes), "counts": "log-uniform in [4096, 65536], seed 7",
@@ -542,7 +547,7 @@ def rollout(args) -> None:
             "forward_ms": f, "backward_ms": bk, "plain_steps_ms": pl,
             "forward_us_per_substep": 1e3 * f / substeps, "backward_us_per_substep": 1e3 * bk / substeps,
             "rollouts": args.rollouts, "warmup": args.warmup_rollouts, "gpu_launches": int(launches),
-            "forward_blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity"], blocks)),
+            "forward_blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm", "balance"], blocks)),
             "loss": loss, "grad_norms": {"v0": float(np.linalg.norm(dv[:, :3])), "c": float(dc),
                                          "g": [float(v) for v in dg]},
             "memory_bytes": {"tape_one_segment": tape_bytes, "checkpoints": (substeps // every + 1) * 36 * n},

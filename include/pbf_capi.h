@@ -358,15 +358,23 @@ int pbf_render_read(pbf_ctx* ctx, int which, float* rgba);
 
 /* ------------------------------------------------------------ autotuner -- */
 
-/* Threads per block of the five neighbour kernels, in the order friends,
-   density (scaling), delta, viscosity, vorticity.  Results do not depend on
-   them; set requires multiples of 32 in [32, 512]. */
+/* The launch shape, PBF_LAUNCH_SHAPE_FIELDS ints: threads per block of the
+   five neighbour kernels in the order friends, density (scaling), delta,
+   viscosity, vorticity (multiples of 32 in [32, 512]), then the friends
+   algorithm (0: one thread scans the 27 cells per particle; 1: a warp scans
+   the cells of each run of same-cell particles together), then the balance
+   flag (1: the four solver passes hand each block's particles to its threads
+   in decreasing order of friend count, so warps walk lists of similar
+   length).  Results do not depend on any of them. */
+#define PBF_LAUNCH_SHAPE_FIELDS 7
 int pbf_get_launch_shape(pbf_ctx* ctx, int* blocks);
 int pbf_set_launch_shape(pbf_ctx* ctx, const int* blocks);
 
 /* Time `trial_substeps` substeps from the current state for each candidate
-   block size (64, 128, 256, 512), keep the fastest per kernel, restore the
-   state, and report the choice through blocks_out (5 ints, may be NULL). */
+   block size (64, 128, 256, 512), both friends algorithms and both balance
+   settings, keep the fastest per kernel (the balance setting by the sum of
+   the solver passes), restore the state, and report the choice through
+   blocks_out (PBF_LAUNCH_SHAPE_FIELDS ints, may be NULL). */
 int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out);
 
 /* ------------------------------------------------------------- scenarios -- */

@@ -429,7 +429,8 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     mark("updateCells");
     pbf::launch_update_cells(c.n, keys, ctx->cells, s);
     mark("buildFriendsList");
-    pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, meta, ctx->errWord, ls.friends, s);
+    pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, meta, ctx->errWord, ls.friends,
+                              ls.friendsAlgorithm, s);
     mark("resetPartList");
     pbf::launch_reset_cells(c.n, keys, ctx->cells, s);
     launched += 3;
@@ -438,11 +439,11 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     for (unsigned it = 0; it < iters; ++it) {
         float4* packed = tape ? tape->q[it] : ctx->pred[a ^ 1];
         mark("computeScaling", (int)it);
-        pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, ls.scaling, s);
+        pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, ls.scaling, ls.balance, s);
         mark("computeDelta", (int)it);
         pbf::launch_compute_delta(c, b, packed, ctx->pos[sortedPos], ctx->pred[a], ctx->density, list, meta,
                                   it + 1 == iters, tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr,
-                                  ls.delta, s);
+                                  ls.delta, ls.balance, s);
         launched += 2;
     }
     if (iters == 0) {  // packData with the density buffer as it stands (src/Simulation.cpp:591)
@@ -456,9 +457,9 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
                                   paused ? nullptr : ctx->idsTmp, ctx->ids, s);
     if (tape) cudaMemcpyAsync(tape->v2, ctx->vel[V], v4, cudaMemcpyDeviceToDevice, s);
     mark("applyViscosity");
-    pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, ls.viscosity, s);
+    pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, ls.viscosity, ls.balance, s);
     mark("applyVorticity");
-    pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, ls.vorticity, s);
+    pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, ls.vorticity, ls.balance, s);
     launched += 3;
     PBF_CUDA(ctx, cudaGetLastError());
     ctx->curPos = sortedPos ^ 1;
@@ -1262,6 +1263,8 @@ int pbf_get_launch_shape(pbf_ctx* ctx, int* blocks) {
     if (!ctx || !blocks) return fail(ctx, PBF_ERR_INVALID, "pbf_get_launch_shape: NULL argument");
     const pbf::LaunchShape& s = ctx->shape;
     blocks[0] = s.friends; blocks[1] = s.scaling; blocks[2] = s.delta; blocks[3] = s.viscosity; blocks[4] = s.vorticity;
+    blocks[5] = s.friendsAlgorithm;
+    blocks[6] = s.balance;
     return PBF_OK;
 }
 
@@ -1270,8 +1273,11 @@ int pbf_set_launch_shape(pbf_ctx* ctx, const int* blocks) {
     for (int k = 0; k < 5; ++k)
         if (blocks[k] < 32 || blocks[k] > pbf::kMaxBlock || blocks[k] % 32)
             return fail(ctx, PBF_ERR_INVALID, "block sizes must be multiples of 32 in [32, 512]");
+    if (blocks[5] != 0 && blocks[5] != 1) return fail(ctx, PBF_ERR_INVALID, "the friends algorithm is 0 or 1");
+    if (blocks[6] != 0 && blocks[6] != 1) return fail(ctx, PBF_ERR_INVALID, "the balance flag is 0 or 1");
     ctx->shape.friends = blocks[0]; ctx->shape.scaling = blocks[1]; ctx->shape.delta = blocks[2];
-    ctx->shape.viscosity = blocks[3]; ctx->shape.vorticity = blocks[4];
+    ctx->shape.viscosity = blocks[3]; ctx->shape.vorticity = blocks[4]; ctx->shape.friendsAlgorithm = blocks[5];
+    ctx->shape.balance = blocks[6];
     drop_graph(ctx);
     return PBF_OK;
 }
@@ -1313,11 +1319,19 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
     };
     const char* names[5] = {"buildFriendsList", "computeScaling", "computeDelta", "applyViscosity", "applyVorticity"};
     const int candidates[4] = {64, 128, 256, 512};
-    float best[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
-    int choice[5] = {256, 256, 256, 256, 256};
+    // friends: best over block size x algorithm; the solver passes: best
+    // block size per balance setting, then the balance setting with the
+    // smaller sum
+    float friendsMs = 1e30f;
+    int friendsBlock = shape0.friends, algorithm = shape0.friendsAlgorithm;
+    float solverMs[2][4];
+    int solverBlock[2][4];
+    for (int bal = 0; bal < 2; ++bal)
+        for (int q = 0; q < 4; ++q) { solverMs[bal][q] = 1e30f; solverBlock[bal][q] = 256; }
     ctx->stageTiming = true;
-    for (int cand : candidates) {
-        ctx->shape = pbf::LaunchShape{cand, cand, cand, cand, cand};
+    for (int trial = 0; trial < 16; ++trial) {
+        const int cand = candidates[trial % 4], algo = (trial / 4) & 1, bal = trial / 8;
+        ctx->shape = pbf::LaunchShape{cand, cand, cand, cand, cand, algo, bal};
         ctx->stageNames.clear();
         ctx->stageMs.clear();
         StageClock clock{ctx, {}};
@@ -1326,9 +1340,19 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
         restore();
         if (rc != PBF_OK) break;
         for (int q = 0; q < 5; ++q)
-            for (size_t k = 0; k < ctx->stageNames.size(); ++k)
-                if (ctx->stageNames[k] == names[q] && ctx->stageMs[k] < best[q]) { best[q] = ctx->stageMs[k]; choice[q] = cand; }
+            for (size_t k = 0; k < ctx->stageNames.size(); ++k) {
+                if (ctx->stageNames[k] != names[q]) continue;
+                const float ms = ctx->stageMs[k];
+                if (q == 0 && ms < friendsMs) { friendsMs = ms; friendsBlock = cand; algorithm = algo; }
+                if (q > 0 && ms < solverMs[bal][q - 1]) { solverMs[bal][q - 1] = ms; solverBlock[bal][q - 1] = cand; }
+            }
     }
+    float sum[2] = {0.0f, 0.0f};
+    for (int bal = 0; bal < 2; ++bal)
+        for (int q = 0; q < 4; ++q) sum[bal] += solverMs[bal][q];
+    const int balance = sum[1] <= sum[0] ? 1 : 0;
+    int choice[5] = {friendsBlock, solverBlock[balance][0], solverBlock[balance][1], solverBlock[balance][2],
+                     solverBlock[balance][3]};
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     release();
     ctx->stageTiming = timing0;
@@ -1339,8 +1363,12 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
     drop_graph(ctx);
     if (rc != PBF_OK) { ctx->shape = shape0; return rc; }
     if (e != cudaSuccess) { ctx->shape = shape0; return fail(ctx, PBF_ERR_CUDA, std::string("pbf_autotune: ") + cudaGetErrorString(e)); }
-    ctx->shape = pbf::LaunchShape{choice[0], choice[1], choice[2], choice[3], choice[4]};
-    if (blocks_out) for (int q = 0; q < 5; ++q) blocks_out[q] = choice[q];
+    ctx->shape = pbf::LaunchShape{choice[0], choice[1], choice[2], choice[3], choice[4], algorithm, balance};
+    if (blocks_out) {
+        for (int q = 0; q < 5; ++q) blocks_out[q] = choice[q];
+        blocks_out[5] = algorithm;
+        blocks_out[6] = balance;
+    }
     return read_error_word(ctx);
 }
 

@@ -72,6 +72,8 @@ SceneParams make_scene_params(const PbfParameters& p, uint32_t keyBase);
 // Threads per block of the kernels whose block size the autotuner chooses.
 struct LaunchShape {
     int friends = 256, scaling = 256, delta = 256, viscosity = 256, vorticity = 256;
+    int friendsAlgorithm = 0;  // 0: one thread scans per particle; 1: warp-cooperative runs
+    int balance = 0;           // solver passes: threads take the block's particles by friend count
 };
 constexpr int kMaxBlock = 512;
 
@@ -84,20 +86,21 @@ void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const 
                           float4* posOut, float4* predOut, uint32_t* idsOut, cudaStream_t s);
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
+// algorithm: LaunchShape::friendsAlgorithm
 void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint2* meta, int* errorWord, int block, cudaStream_t s);
+                          uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s);
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
-                            const uint32_t* list, const uint2* meta, int block, cudaStream_t s);
+                            const uint32_t* list, const uint2* meta, int block, int balance, cudaStream_t s);
 // posPrev: the sorted positions, read only by the force planes.
 void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, const float4* posPrev,
                           float4* predOut, const float* density, const uint32_t* list, const uint2* meta,
-                          int lastIteration, uint8_t* clampMask, int block, cudaStream_t s);
+                          int lastIteration, uint8_t* clampMask, int block, int balance, cudaStream_t s);
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
                               float4* vel, const uint32_t* idsIn, uint32_t* idsOut, cudaStream_t s);
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
-                            float4* omega, const uint32_t* list, const uint2* meta, int block, cudaStream_t s);
+                            float4* omega, const uint32_t* list, const uint2* meta, int block, int balance, cudaStream_t s);
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
-                            float4* velOut, const uint32_t* list, const uint2* meta, int block, cudaStream_t s);
+                            float4* velOut, const uint32_t* list, const uint2* meta, int block, int balance, cudaStream_t s);
 
 // ---- radix sort (pbf_sort.cu) ----
 struct SortPlan {

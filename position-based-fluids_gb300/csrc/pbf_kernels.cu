@@ -217,6 +217,165 @@ build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, cons
     meta[i] = make_uint2((uint32_t)mt, (uint32_t)(mt >> 32));
 }
 
+// The same lists, built warp-cooperatively.  A warp takes its 32 particles
+// run by run (a run: consecutive particles in one cell of one scene, which
+// share the 27-cell candidate sequence).  Lanes take 32 candidates of the
+// run's sequence at a time, in order (the candidate of lane L follows that of
+// lane L-1), and every run member tests all 32: its accepted candidates are
+// appended to their circles in sequence order, with ranks from the circle
+// counts and match_any, so the lists equal those of the per-particle scan
+// while every lane stays busy.  Circle counts saturate at perCircle.
+__global__ void __launch_bounds__(kMaxBlock)
+build_friends_warp_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const uint2* __restrict__ cells,
+                          uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int warpBase = i - lane;
+    const int n = c.n;
+    if (warpBase >= n) return;  // whole warp idle
+    const bool valid = i < n;
+    const float4 pi = valid ? pred[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const int cx = __float2int_rz(pi.x / c.h), cy = __float2int_rz(pi.y / c.h), cz = __float2int_rz(pi.z / c.h);
+    const uint32_t base = valid ? key_base(b, i) : 0u;
+    const int C = c.circles, P = c.perCircle;
+    const bool pow2 = (c.grid & (c.grid - 1)) == 0;
+    const uint32_t gmask = c.grid - 1;
+    const int ux = __shfl_up_sync(kFull, cx, 1), uy = __shfl_up_sync(kFull, cy, 1), uz = __shfl_up_sync(kFull, cz, 1);
+    const uint32_t ub = __shfl_up_sync(kFull, base, 1);
+    const bool head = valid && (lane == 0 || cx != ux || cy != uy || cz != uz || base != ub);
+    uint32_t heads = __ballot_sync(kFull, head);
+    const uint32_t validMask = __ballot_sync(kFull, valid);
+    const uint32_t ltMask = (1u << lane) - 1u;
+    const uint32_t capP = (uint32_t)P * 0x01010101u;
+    uint32_t cntLo = 0, cntHi = 0;  // this lane's particle: 8 circles x 8-bit counters
+    while (heads) {
+        const int h0 = __ffs(heads) - 1;
+        heads &= heads - 1;
+        const int h1 = heads ? __ffs(heads) - 1 : 32;
+        const uint32_t upTo = h1 == 32 ? kFull : ((1u << h1) - 1u);
+        const uint32_t runMask = validMask & upTo & ~((1u << h0) - 1u);
+        const int rx0 = __shfl_sync(kFull, cx, h0), ry0 = __shfl_sync(kFull, cy, h0), rz0 = __shfl_sync(kFull, cz, h0);
+        const uint32_t rbase = __shfl_sync(kFull, base, h0);
+        // lane q < 27: neighbour cell q in the scan order (x, then y, then z offsets)
+        uint32_t start = 0, count = 0;
+        if (lane < 27) {
+            const int x = lane / 9 - 1, y = (lane / 3) % 3 - 1, z = lane % 3 - 1;
+            const uint32_t m = expand_bits(rx0 + x) | (expand_bits(ry0 + y) << 1) | (expand_bits(rz0 + z) << 2);
+            const uint2 range = cells[rbase + (pow2 ? (m & gmask) : (m % c.grid))];
+            if (range.x != kEmpty) {
+                const uint32_t last = min(range.y, (uint32_t)(n - 1));
+                if (range.x > last) atomicOr(err, 1);
+                else { start = range.x; count = last - range.x + 1u; }
+            }
+        }
+        uint32_t end = count;  // inclusive scan: candidates up to and including cell q
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(kFull, end, d);
+            if (lane >= d) end += v;
+        }
+        const uint32_t total = __shfl_sync(kFull, end, 31);
+        for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+            const uint32_t t = t0 + (uint32_t)lane;
+            const bool tv = t < total;
+            int q = 0;  // the first cell with end > t
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) {
+                const uint32_t e = __shfl_sync(kFull, end, q + s - 1);
+                if (e <= t) q += s;
+            }
+            const uint32_t qs = __shfl_sync(kFull, start, q), qe = __shfl_sync(kFull, end, q);
+            const uint32_t qc = __shfl_sync(kFull, count, q);
+            const uint32_t j = qs + (t - (qe - qc));
+            const float4 pj = tv ? __ldg(pred + j) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            for (uint32_t rm = runMask; rm; rm &= rm - 1u) {
+                const int pl = __ffs(rm) - 1;
+                const int ip = warpBase + pl;
+                const float px = __shfl_sync(kFull, pi.x, pl), py = __shfl_sync(kFull, pi.y, pl);
+                const float pz = __shfl_sync(kFull, pi.z, pl);
+                const float rx = px - pj.x, ry = py - pj.y, rz = pz - pj.z;
+                const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+                const bool acc = tv && (int)j != ip && !(r2 >= c.h2);  // NaN distances are kept, as in the scan
+                const uint32_t am = __ballot_sync(kFull, acc);
+                if (!am) continue;
+                int circ = (r2 >= c.circT[0]) + (r2 >= c.circT[1]) + (r2 >= c.circT[2]) + (r2 >= c.circT[3]);
+                if (C > 5) circ += (r2 >= c.circT[4]) + (r2 >= c.circT[5]) + (r2 >= c.circT[6]);
+                const uint32_t plo = __shfl_sync(kFull, cntLo, pl), phi = __shfl_sync(kFull, cntHi, pl);
+                if (acc) {
+                    const uint32_t peers = __match_any_sync(am, circ);
+                    const uint32_t have = circ < 4 ? (plo >> (8 * circ)) & 0xFFu : (phi >> (8 * (circ - 4))) & 0xFFu;
+                    const uint32_t rank = have + (uint32_t)__popc(peers & ltMask);
+                    if ((int)rank < P) list[(size_t)(circ * P + (int)rank) * n + ip] = j;
+                }
+                const uint32_t incLo = (acc && circ < 4) ? 1u << (8 * circ) : 0u;
+                const uint32_t incHi = (acc && circ >= 4) ? 1u << (8 * (circ - 4)) : 0u;
+                const uint32_t sLo = __reduce_add_sync(kFull, incLo), sHi = __reduce_add_sync(kFull, incHi);
+                if (lane == pl) {  // bytes stay below 256 (<= 64 + 32), then saturate at perCircle
+                    cntLo = __vminu4(plo + sLo, capP);
+                    cntHi = __vminu4(phi + sHi, capP);
+                }
+            }
+        }
+    }
+    if (!valid) return;
+    const uint64_t cnt = (uint64_t)cntLo | ((uint64_t)cntHi << 32);
+    int total = 0;
+    uint64_t mt = 0;
+    for (int k = 0; k < C; ++k) {
+        total += (int)byte_of(cnt, k);
+        mt |= (uint64_t)byte_of(cnt, k) << (7 * k);
+    }
+    mt |= (uint64_t)circles_kept(cnt, C, total, 0.6f) << 56;
+    mt |= (uint64_t)circles_kept(cnt, C, total, 0.5f) << 60;
+    meta[i] = make_uint2((uint32_t)mt, (uint32_t)(mt >> 32));
+}
+
+// ------------------------------------------------- balanced thread map --
+// The block's particles handed to its threads in decreasing order of their
+// friend count, so that the lanes of a warp walk lists of similar length;
+// a particle's result does not depend on which thread computes it.  Counting
+// sort in shared memory over the kept-circle count (saturated at 255), ties
+// in any order.  Every thread of the block must call it (it synchronises);
+// returns the particle index, or -1 for threads beyond the block's particles.
+__device__ __forceinline__ int balanced_particle(const uint2* __restrict__ meta, int n, bool densityPass) {
+    __shared__ uint32_t bins[256];
+    __shared__ int order[kMaxBlock];
+    const int t = threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + t;
+    for (int k = t; k < 256; k += blockDim.x) bins[k] = 0u;
+    __syncthreads();
+    int key = -1;
+    if (i < n) {
+        const uint64_t mt = load_meta(meta, i);
+        const int kept = densityPass ? kept_density(mt) : kept_other(mt);
+        int tot = 0;
+        for (int c = 0; c < kept; ++c) tot += (int)circle_count(mt, c);
+        key = 255 - min(tot, 255);
+        atomicAdd(&bins[key], 1u);
+    }
+    __syncthreads();
+    if (t < 32) {  // exclusive scan of the 256 bins: 8 per lane
+        uint32_t v[8], s = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) { v[k] = bins[8 * t + k]; s += v[k]; }
+        uint32_t incl = s;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (t >= d) incl += u;
+        }
+        uint32_t run = incl - s;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) { bins[8 * t + k] = run; run += v[k]; }
+    }
+    __syncthreads();
+    if (key >= 0) order[atomicAdd(&bins[key], 1u)] = i;
+    __syncthreads();
+    const int valid = min(n - (int)(blockIdx.x * blockDim.x), (int)blockDim.x);
+    return t < valid ? order[t] : -1;
+}
+
 // -------------------------------------------------------------- scaling --
 // Relaxed variants (R = true, relaxedMath): per pair one reciprocal square
 // root w = 1/|r| replaces sqrt(r^2) and the divisions by |r|, and sums are
@@ -230,14 +389,14 @@ __device__ __forceinline__ float spiky_over_r(const DevConsts& c, float r2, floa
 }
 
 // compute_scaling.cl:27-112 followed by pack_data.cl (w = lambda).
-template <bool R>
+template <bool R, bool B>
 __global__ void __launch_bounds__(kMaxBlock)
 compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __restrict__ predPacked,
                        float* __restrict__ density, const uint32_t* __restrict__ list,
                        const uint2* __restrict__ meta) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
-    if (i >= n) return;
+    const int i = B ? balanced_particle(meta, n, true) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < 0 || i >= n) return;
     const float4 pi = pred[i];
     const uint64_t mt = load_meta(meta, i);
     float ds = 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
@@ -287,14 +446,14 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
 // the optional box clamp on `future`, then update_predicted.cl.  After the
 // last iteration w carries the density (pack_data.cl with the density source,
 // src/Simulation.cpp:591).
-template <bool R>
+template <bool R, bool B>
 __global__ void __launch_bounds__(kMaxBlock)
 compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const float4* __restrict__ posPrev,
                      float4* __restrict__ predOut, const float* __restrict__ density, const uint32_t* __restrict__ list,
                      const uint2* __restrict__ meta, int lastIteration, uint8_t* __restrict__ clampMask) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
-    if (i >= n) return;
+    const int i = B ? balanced_particle(meta, n, false) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < 0 || i >= n) return;
     const float4 pi = pp[i];
     const uint64_t mt = load_meta(meta, i);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
@@ -391,14 +550,14 @@ __global__ void update_velocities_kernel(DevConsts c, const float4* __restrict__
 
 // apply_viscosity.cl:12-86, every neighbour read from the pre-pass
 // velocities (Jacobi).
-template <bool R>
+template <bool R, bool B>
 __global__ void __launch_bounds__(kMaxBlock)
 apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const float4* __restrict__ velIn,
                        float4* __restrict__ velOut, float4* __restrict__ omega,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
-    if (i >= n) return;
+    const int i = B ? balanced_particle(meta, n, false) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < 0 || i >= n) return;
     const float4 pi = pred[i], vi = velIn[i];
     const uint64_t mt = load_meta(meta, i);
     float vsx = 0.0f, vsy = 0.0f, vsz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
@@ -446,14 +605,14 @@ apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, co
 }
 
 // apply_vorticity.cl:12-86
-template <bool R>
+template <bool R, bool B>
 __global__ void __launch_bounds__(kMaxBlock)
 apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
                        const float4* __restrict__ velIn, float4* __restrict__ velOut,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = c.n;
-    if (i >= n) return;
+    const int i = B ? balanced_particle(meta, n, false) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < 0 || i >= n) return;
     const float4 pi = pred[i];
     const uint64_t mt = load_meta(meta, i);
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
@@ -538,21 +697,23 @@ void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream
 }
 
 void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint2* meta, int* errorWord, int block, cudaStream_t s) {
-    build_friends_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, reinterpret_cast<const uint2*>(cells),
-                                                                  list, meta, errorWord);
+                          uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s) {
+    auto k = algorithm == 1 ? build_friends_warp_kernel : build_friends_kernel;
+    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, reinterpret_cast<const uint2*>(cells), list, meta, errorWord);
 }
 
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
-                            const uint32_t* list, const uint2* meta, int block, cudaStream_t s) {
-    auto k = c.relaxed ? compute_scaling_kernel<true> : compute_scaling_kernel<false>;
+                            const uint32_t* list, const uint2* meta, int block, int balance, cudaStream_t s) {
+    auto k = c.relaxed ? (balance ? compute_scaling_kernel<true, true> : compute_scaling_kernel<true, false>)
+                       : (balance ? compute_scaling_kernel<false, true> : compute_scaling_kernel<false, false>);
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, predPacked, density, list, meta);
 }
 
 void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, const float4* posPrev,
                           float4* predOut, const float* density, const uint32_t* list, const uint2* meta,
-                          int lastIteration, uint8_t* clampMask, int block, cudaStream_t s) {
-    auto k = c.relaxed ? compute_delta_kernel<true> : compute_delta_kernel<false>;
+                          int lastIteration, uint8_t* clampMask, int block, int balance, cudaStream_t s) {
+    auto k = c.relaxed ? (balance ? compute_delta_kernel<true, true> : compute_delta_kernel<true, false>)
+                       : (balance ? compute_delta_kernel<false, true> : compute_delta_kernel<false, false>);
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, predPacked, posPrev, predOut, density, list, meta, lastIteration,
                                                clampMask);
 }
@@ -563,14 +724,16 @@ void launch_update_velocities(const DevConsts& c, const float4* pred, const floa
 }
 
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
-                            float4* omega, const uint32_t* list, const uint2* meta, int block, cudaStream_t s) {
-    auto k = c.relaxed ? apply_viscosity_kernel<true> : apply_viscosity_kernel<false>;
+                            float4* omega, const uint32_t* list, const uint2* meta, int block, int balance, cudaStream_t s) {
+    auto k = c.relaxed ? (balance ? apply_viscosity_kernel<true, true> : apply_viscosity_kernel<true, false>)
+                       : (balance ? apply_viscosity_kernel<false, true> : apply_viscosity_kernel<false, false>);
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, velIn, velOut, omega, list, meta);
 }
 
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
-                            float4* velOut, const uint32_t* list, const uint2* meta, int block, cudaStream_t s) {
-    auto k = c.relaxed ? apply_vorticity_kernel<true> : apply_vorticity_kernel<false>;
+                            float4* velOut, const uint32_t* list, const uint2* meta, int block, int balance, cudaStream_t s) {
+    auto k = c.relaxed ? (balance ? apply_vorticity_kernel<true, true> : apply_vorticity_kernel<true, false>)
+                       : (balance ? apply_vorticity_kernel<false, true> : apply_vorticity_kernel<false, false>);
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta);
 }
 

@@ -461,16 +461,18 @@ class Simulation:
         return out
 
     def launch_shape(self) -> list:
-        b = (c_int * 5)()
+        b = (c_int * 7)()
         _check(self.lib.pbf_get_launch_shape(self._ctx, b), self._ctx)
         return list(b)
 
     def set_launch_shape(self, blocks) -> None:
-        b = (c_int * 5)(*blocks)
+        blocks = list(blocks)
+        blocks += self.launch_shape()[len(blocks):]
+        b = (c_int * 7)(*blocks)
         _check(self.lib.pbf_set_launch_shape(self._ctx, b), self._ctx)
 
     def autotune(self, trial_substeps: int = 2) -> list:
-        b = (c_int * 5)()
+        b = (c_int * 7)()
         _check(self.lib.pbf_autotune(self._ctx, trial_substeps, b), self._ctx)
         return list(b)
 

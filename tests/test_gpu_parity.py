@@ -52,9 +52,11 @@ def assert_same(name, got, want):
         raise AssertionError(f"{name}: {nbad} words differ (rel err {rel:.3e}, NaN mismatches {nan_mismatch})")
 
 
-def run_gpu(pbf, params, pos, vel, substeps, device, graph=True, friends=True):
+def run_gpu(pbf, params, pos, vel, substeps, device, graph=True, friends=True, algorithm=None):
     with pbf.Simulation.create(params, pos, vel, device=device) as sim:
         sim.use_graph(graph)
+        if algorithm is not None:  # friends algorithm, and the balanced map with the warp one
+            sim.set_launch_shape(sim.launch_shape()[:5] + [algorithm, algorithm])
         sim.Step(substeps)
         p, v, pr = sim.read_state()
         counts, lst = sim.read_friends() if friends else (None, None)
@@ -112,11 +114,13 @@ def test_sort_at_full_scale_properties(pbf_mod, oracle_mod, cuda_device):
 MANIFEST = json.loads((GOLDEN / "golden.json").read_text())
 
 
+@pytest.mark.parametrize("algorithm", [0, 1], ids=["scan", "warp"])
 @pytest.mark.parametrize("case", MANIFEST["cases"], ids=[c["name"] for c in MANIFEST["cases"]])
-def test_gpu_matches_reference_kernel_digests(case, pbf_mod, cuda_device):
+def test_gpu_matches_reference_kernel_digests(case, algorithm, pbf_mod, cuda_device):
     """Outputs of the reference's own kernels (tests/golden) reproduced on the GPU."""
     params, pos, vel = mg().scene(tuple(case["block"]), case["overrides"])
-    p, v, pr, _, _ = run_gpu(pbf_mod, params, pos, vel, case["substeps"], cuda_device, friends=False)
+    p, v, pr, _, _ = run_gpu(pbf_mod, params, pos, vel, case["substeps"], cuda_device, friends=False,
+                             algorithm=algorithm)
     for name, arr in (("pos", p), ("vel", v), ("pred", pr)):
         assert mg().digest(arr) == case["sha256"][name], f"{case['name']}: {name}"
 
@@ -135,13 +139,16 @@ SUBSTEP_CASES = {
 }
 
 
+@pytest.mark.parametrize("algorithm", [0, 1], ids=["scan", "warp"])
 @pytest.mark.parametrize("name", list(SUBSTEP_CASES))
-def test_substeps_bit_exact(name, pbf_mod, oracle_mod, cuda_device):
+def test_substeps_bit_exact(name, algorithm, pbf_mod, oracle_mod, cuda_device):
+    """Both friends algorithms (per-particle scan, warp-cooperative runs),
+    with the plain and the balanced thread map of the solver passes."""
     spec, substeps = SUBSTEP_CASES[name]
     spec = dict(spec)
     dims = spec.pop("dims")
     params, pos, vel = scene(pbf_mod, dims, **spec)
-    gp, gv, gpr, gcounts, glist = run_gpu(pbf_mod, params, pos, vel, substeps, cuda_device)
+    gp, gv, gpr, gcounts, glist = run_gpu(pbf_mod, params, pos, vel, substeps, cuda_device, algorithm=algorithm)
     op, ov, opr, dbg = oracle_mod.step(params, pos, vel, substeps, debug=True)
     assert np.array_equal(gcounts, dbg["counts"]), "friend counts"
     slots = int(dbg["counts"][:, 0].max()) if len(dbg["counts"]) else 0
