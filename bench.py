@@ -245,16 +245,18 @@ def gpu_arm(args) -> None:
     hvel = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
     sim.read_state_into(hpos.data_ptr(), hvel.data_ptr())
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    def e2e_frame():  # upload, step, download through the C-ABI; one wait per frame
+        sim.write_state_async(hpos.data_ptr(), hvel.data_ptr())
+        sim.step_async(sub)
+        sim.read_state_async(hpos.data_ptr(), hvel.data_ptr())
+        sim.synchronize()
+
     for _ in range(3):
-        sim.write_state_from(hpos.data_ptr(), hvel.data_ptr())
-        sim.Step(sub)
-        sim.read_state_into(hpos.data_ptr(), hvel.data_ptr())
+        e2e_frame()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        sim.write_state_from(hpos.data_ptr(), hvel.data_ptr())
-        sim.Step(sub)
-        sim.read_state_into(hpos.data_ptr(), hvel.data_ptr())
+        e2e_frame()
     e2e_s = time.perf_counter() - t0
     t = torch.tensor([e2e_s], device="cuda")
     if dist is not None:

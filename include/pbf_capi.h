@@ -175,6 +175,14 @@ int pbf_load_state(pbf_ctx* ctx, const char* path);
    (pbf_read_ids). */
 int pbf_write_state(pbf_ctx* ctx, const float* pos, const float* vel);
 
+/* pbf_write_state / pbf_read_state enqueued on the context's stream without
+   waiting: with page-locked host memory the copies run in stream order with
+   the steps around them, and pbf_synchronize waits for all of it (a frame
+   loop: write_async, step_async, read_async, synchronize).  The host memory
+   must stay valid until then. */
+int pbf_write_state_async(pbf_ctx* ctx, const float* pos, const float* vel);
+int pbf_read_state_async(pbf_ctx* ctx, float* pos, float* vel, float* pred);
+
 /* Device address of the current positions (float4 x particleCount), valid
    until the next step.  Headless replacement of the GL buffer IDs
    mSharedPingBufferID / mSharedPongBufferID (src/Simulation.hpp:130-135). */

@@ -384,6 +384,11 @@ struct StageClock {
     }
 };
 
+__global__ void iota_kernel(int n, uint32_t* ids) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) ids[i] = (uint32_t)i;
+}
+
 __global__ void pack_density_kernel(int n, float4* pred, const float* density) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) pred[i].w = density[i];
@@ -688,9 +693,8 @@ int pbf_init_buffers(pbf_ctx* ctx, const float* init_pos, const float* init_vel)
         (rc = dev_alloc(ctx, &ctx->ids, n)) || (rc = dev_alloc(ctx, &ctx->idsTmp, n)))
         return rc;
     {
-        std::vector<uint32_t> iota(n);
-        for (int i = 0; i < n; ++i) iota[i] = (uint32_t)i;
-        PBF_CUDA(ctx, cudaMemcpy(ctx->ids, iota.data(), 4 * (size_t)n, cudaMemcpyHostToDevice));
+        iota_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, ctx->ids);
+        PBF_CUDA(ctx, cudaGetLastError());
     }
     PBF_CUDA(ctx, cudaMemset(ctx->omega, 0, 16 * (size_t)n));
     PBF_CUDA(ctx, cudaMemset(ctx->density, 0, 4 * (size_t)n));
@@ -1086,20 +1090,36 @@ int pbf_read_state(pbf_ctx* ctx, float* pos, float* vel, float* pred) {
     return PBF_OK;
 }
 
-int pbf_write_state(pbf_ctx* ctx, const float* pos, const float* vel) {
+int pbf_write_state_async(pbf_ctx* ctx, const float* pos, const float* vel) {
     if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
     if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers has not run");
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
     const size_t bytes = 16 * (size_t)ctx->n;
-    std::vector<uint32_t> iota;
     if (pos) {
         PBF_CUDA(ctx, cudaMemcpyAsync(ctx->pos[ctx->curPos], pos, bytes, cudaMemcpyHostToDevice, ctx->stream));
-        iota.resize(ctx->n);  // the written records become particles 0 .. N-1
-        for (int i = 0; i < ctx->n; ++i) iota[i] = (uint32_t)i;
-        PBF_CUDA(ctx, cudaMemcpyAsync(ctx->ids, iota.data(), 4 * (size_t)ctx->n, cudaMemcpyHostToDevice, ctx->stream));
+        // the written records become particles 0 .. N-1
+        iota_kernel<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->ids);
+        PBF_CUDA(ctx, cudaGetLastError());
     }
     if (vel) PBF_CUDA(ctx, cudaMemcpyAsync(ctx->vel[ctx->curVel], vel, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return PBF_OK;
+}
+
+int pbf_write_state(pbf_ctx* ctx, const float* pos, const float* vel) {
+    int rc = pbf_write_state_async(ctx, pos, vel);
+    if (rc) return rc;
     PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PBF_OK;
+}
+
+int pbf_read_state_async(pbf_ctx* ctx, float* pos, float* vel, float* pred) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    if (!ctx->buffersReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers has not run");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = 16 * (size_t)ctx->n;
+    if (pos) PBF_CUDA(ctx, cudaMemcpyAsync(pos, ctx->pos[ctx->curPos], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vel) PBF_CUDA(ctx, cudaMemcpyAsync(vel, ctx->vel[ctx->curVel], bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (pred) PBF_CUDA(ctx, cudaMemcpyAsync(pred, ctx->pred[ctx->curPred], bytes, cudaMemcpyDeviceToHost, ctx->stream));
     return PBF_OK;
 }
 

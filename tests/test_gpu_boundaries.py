@@ -89,3 +89,25 @@ def test_perf_trackers_follow_the_reference_monitor(pbf_mod, cuda_device):
         assert total >= 0.5 * first[name][3] - 1e-9
     assert [t["eventName"] for t in doc["trackers"]] == want
     assert abs(doc["total_time"] - sum(t[3] for t in second)) < 1e-3
+
+
+def test_async_state_copies_match_sync(pbf_mod, cuda_device):
+    """write_state_async / step_async / read_state_async / synchronize gives
+    the frames the synchronous calls give."""
+    torch = pytest.importorskip("torch")
+    params, pos, vel = pbf_mod.make_scene("dam_break_32k")
+    n = len(pos)
+    hp = torch.from_numpy(pos.copy()).pin_memory()
+    hv = torch.zeros((n, 4), dtype=torch.float32).pin_memory()
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as a, \
+         pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as b:
+        p, v = pos.copy(), vel.copy()
+        for _ in range(3):
+            a.write_state(p, v)
+            a.Step(2)
+            p, v, _ = a.read_state()
+            b.write_state_async(hp.data_ptr(), hv.data_ptr())
+            b.step_async(2)
+            b.read_state_async(hp.data_ptr(), hv.data_ptr())
+            b.synchronize()
+        assert _same(p, hp.numpy()) and _same(v, hv.numpy())
