@@ -190,6 +190,20 @@ def reference_arm(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def replica_rate(units: float, seconds: float, dist=None, device: str = "cpu") -> tuple[float, float]:
+    """Whole-job rate of replicas: the units of all ranks over the slowest
+    rank's time.  Returns (rate, slowest seconds); without a process group,
+    this rank's own."""
+    import torch
+    if dist is None:
+        return units / seconds, seconds
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(u.item()) / float(t.item()), float(t.item())
+
+
 def gpu_arm(args) -> None:
     import numpy as np
     import torch
@@ -234,11 +248,8 @@ def gpu_arm(args) -> None:
     barrier()
     ms = ev0.elapsed_time(ev1)
     launches = sim.launch_count() - launches0
-    t = torch.tensor([ms], device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item())
-    value = world * n * iters * sub * args.steps / (ms / 1000.0)
+    value, ms = replica_rate(n * iters * sub * args.steps, ms / 1000.0, dist, "cuda")
+    ms *= 1000.0
 
     # ---- end to end through the C-ABI with pinned host buffers ----
     hpos = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
@@ -258,10 +269,7 @@ def gpu_arm(args) -> None:
     for _ in range(e2e_steps):
         e2e_frame()
     e2e_s = time.perf_counter() - t0
-    t = torch.tensor([e2e_s], device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = world * n * iters * sub * e2e_steps / float(t.item())
+    e2e_value, _ = replica_rate(n * iters * sub * e2e_steps, e2e_s, dist, "cuda")
 
     # ---- per-stage device times (eager launches, events between stages) ----
     counts, _ = sim.read_friends(slots=1)
