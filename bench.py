@@ -71,7 +71,14 @@ STAGE_BYTES = {
 # DRAM bytes (read + write) of one launch from an ncu capture of the
 # dam_break_1m scene after 50 frames, with the mean list length then; scaled
 # to the measured list length by the stage's algorithmic bytes.
-TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 308.16e6, "nl": 31.19}}
+TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 307.58e6, "nl": 31.19},
+                   "computeDelta": {"bytes": 268.21e6, "nl": 26.99}}
+# Warp instructions of one exact-mode launch from the same capture (256-thread
+# blocks), with its mean list length; scaled by the list length measured.
+ISSUE_CAPTURE = {"computeScaling": {"inst": 163.26e6, "nl": 31.19},
+                 "computeDelta": {"inst": 167.33e6, "nl": 26.99}}
+SM_COUNT = 152
+SCHEDULERS_PER_SM = 4
 
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -93,6 +100,7 @@ class ClockSampler:
         self.device = device_index
         self.proc = None
         self.path = None
+        self._summary = None
 
     def __enter__(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
@@ -103,7 +111,14 @@ class ClockSampler:
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
-        time.sleep(0.3)
+        deadline = time.time() + 3.0  # the first sample before the timed region starts
+        while self.proc is not None and time.time() < deadline:
+            try:
+                if Path(self.path).stat().st_size > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.05)
         return self
 
     def __exit__(self, *exc):
@@ -116,6 +131,11 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self) -> dict:
+        if self._summary is None:
+            self._summary = self._read()
+        return self._summary
+
+    def _read(self) -> dict:
         rows = []
         try:
             for line in Path(self.path).read_text().splitlines():
@@ -295,28 +315,40 @@ def gpu_arm(args) -> None:
         cap = TRAFFIC_CAPTURE[dominant]
         scale = STAGE_BYTES[dominant](nl, nd) / STAGE_BYTES[dominant](cap["nl"], cap["nl"])
         traffic = cap["bytes"] * scale
-    # ---- the other arithmetic mode, same scene state and block sizes ----
-    other = "exact" if args.math == "relaxed" else "relaxed"
-    p2 = params.copy()
-    p2.relaxedMath = 1 if other == "relaxed" else 0
-    sim.set_params(p2)
-    for _ in range(3):
-        sim.step_async(sub)
-    sim.synchronize()
-    other_blocks = sim.autotune(trial_substeps=2) if not args.no_autotune else sim.launch_shape()
-    barrier()
-    o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    o0.record(stream)
-    for _ in range(args.steps):
-        sim.step_async(sub)
-    o1.record(stream)
-    o1.synchronize()
-    other_ms = o0.elapsed_time(o1) / args.steps
-    other_line = {"mode": other, "value": n * iters * sub / (other_ms / 1000.0), "ms_per_step": other_ms,
-                  "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm",
-                                      "balance"], other_blocks))}
-    sim.set_params(params)
-    sim.set_launch_shape(blocks)
+    issue = None
+    if dominant in ISSUE_CAPTURE and args.math == "exact":
+        cap = ISSUE_CAPTURE[dominant]
+        inst = cap["inst"] * ((nl if dominant == "computeScaling" else nd) / cap["nl"])
+        clk = clocks.summary().get("sm_mhz") or 2070.0
+        peak_issue = SM_COUNT * SCHEDULERS_PER_SM * clk * 1e6
+        issue = {"kernel": dominant, "warp_instructions_per_launch": inst,
+                 "achieved": inst / (launch_ms / 1000.0), "peak": peak_issue, "unit": "warp instructions/s",
+                 "frac": inst / (launch_ms / 1000.0) / peak_issue,
+                 "source": "ncu smsp__inst_executed.sum of one launch after 50 frames, scaled by list length"}
+    # ---- the other arithmetic mode, same scene state, its own block sizes ----
+    other_line = None
+    if not args.no_other_mode:
+        other = "exact" if args.math == "relaxed" else "relaxed"
+        p2 = params.copy()
+        p2.relaxedMath = 1 if other == "relaxed" else 0
+        sim.set_params(p2)
+        for _ in range(3):
+            sim.step_async(sub)
+        sim.synchronize()
+        other_blocks = sim.autotune(trial_substeps=2) if not args.no_autotune else sim.launch_shape()
+        barrier()
+        o0, o1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        o0.record(stream)
+        for _ in range(args.steps):
+            sim.step_async(sub)
+        o1.record(stream)
+        o1.synchronize()
+        other_ms = o0.elapsed_time(o1) / args.steps
+        other_line = {"mode": other, "value": n * iters * sub / (other_ms / 1000.0), "ms_per_step": other_ms,
+                      "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm",
+                                          "balance"], other_blocks))}
+        sim.set_params(params)
+        sim.set_launch_shape(blocks)
 
     frame_ms = ms / args.steps
     bytes_sub = (444.0 + 56.0 * iters) * n  # whole-substep compulsory bytes, P = 3 sort passes
@@ -349,9 +381,10 @@ def gpu_arm(args) -> None:
                      "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": launch_ms},
         "pipeline_roofline": {"bytes_per_particle_substep": 444.0 + 56.0 * iters, "achieved": pipeline_gbs,
                               "frac": pipeline_gbs / peak},
+        **({"issue_roofline": issue} if issue else {}),
         "stage_ms_per_step": {k: round(v, 4) for k, v in sorted(stage_ms.items(), key=lambda kv: -kv[1])},
         "neighbours": {"density_pass": nl, "other_passes": nd},
-        "other_mode": other_line,
+        **({"other_mode": other_line} if other_line else {}),
         "clocks": clocks.summary(),
     }
     if base is not None:
@@ -619,6 +652,7 @@ def main() -> None:
     ap.add_argument("--cpu-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default block sizes")
+    ap.add_argument("--no-other-mode", action="store_true", help="skip timing the other arithmetic mode")
     ap.add_argument("--math", choices=["relaxed", "exact"], default="exact",
                     help="relaxedMath of the timed scene (the other mode is timed beside it)")
     ap.add_argument("--sweep", action="store_true", help="particle-count sweep (double dam break) instead")

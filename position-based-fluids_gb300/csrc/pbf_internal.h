@@ -106,7 +106,8 @@ void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4
 struct SortPlan {
     int n = 0;
     int passes = 0;       // 8-bit digits needed for keys < gridBufSize
-    int tiles = 0;        // ceil(n / kSortTile)
+    int rounds = 16;      // keys per thread and tile: 256 x rounds per tile (4 at <= 2^18 keys)
+    int tiles = 0;        // ceil(n / (256 * rounds))
     size_t histWords = 0; // 256 * tiles
 };
 SortPlan make_sort_plan(int n, uint32_t gridBufSize);

@@ -13,8 +13,10 @@
 //               totals
 //   downsweep : per-warp stable ranking with __match_any_sync and per-warp
 //               digit counters in shared memory, then the scatter.
-// A tile is 4096 keys: 8 warps, each owning 512 consecutive keys taken in 16
-// rounds of 32, so (warp, round, lane) order is input order.
+// A tile is 8 warps x kRounds rounds of 32 keys: 4096 keys (16 rounds), or
+// 1024 (4 rounds) at most 2^18 keys, where 4096-key tiles would leave most
+// SMs idle.  Each warp owns consecutive keys taken round by round, so
+// (warp, round, lane) order is input order.
 
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -26,12 +28,12 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kRounds = 16;
-constexpr int kTile = kThreads * kRounds;   // 4096 keys
-constexpr int kWarpKeys = 32 * kRounds;     // 512 keys
+constexpr int kSmallSortKeys = 1 << 18;     // at most this many keys: 4-round tiles
 
+template <int kRounds>
 __global__ void __launch_bounds__(kThreads)
 radix_upsweep_kernel(const uint32_t* __restrict__ keys, int n, int shift, int tiles, uint32_t* __restrict__ hist) {
+    constexpr int kTile = kThreads * kRounds;
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -78,10 +80,13 @@ radix_scan_kernel(uint32_t* __restrict__ hist, int tiles, uint32_t* __restrict__
     if (t == 0) totals[blockIdx.x] = carry;
 }
 
+template <int kRounds>
 __global__ void __launch_bounds__(kThreads)
 radix_downsweep_kernel(const uint32_t* __restrict__ keysIn, const uint32_t* __restrict__ permIn,
                        uint32_t* __restrict__ keysOut, uint32_t* __restrict__ permOut, int n, int shift,
                        int tiles, const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals) {
+    constexpr int kTile = kThreads * kRounds;
+    constexpr int kWarpKeys = 32 * kRounds;
     __shared__ uint32_t warpCount[kWarps][256];
     __shared__ uint32_t digitBase[256];
     __shared__ uint32_t warpSums[kWarps];
@@ -159,7 +164,9 @@ SortPlan make_sort_plan(int n, uint32_t gridBufSize) {
     int bits = 0;
     while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)gridBufSize) ++bits;  // keys <= gridBufSize-1
     p.passes = (bits + 7) / 8;
-    p.tiles = (n + kTile - 1) / kTile;
+    p.rounds = n <= kSmallSortKeys ? 4 : 16;
+    const int tile = kThreads * p.rounds;
+    p.tiles = (n + tile - 1) / tile;
     p.histWords = (size_t)256 * p.tiles + 256;  // per-tile histograms, then the 256 digit totals
     return p;
 }
@@ -172,10 +179,19 @@ int launch_radix_sort(const SortPlan& plan, uint32_t* keys[2], uint32_t* perm[2]
     uint32_t* totals = hist + (size_t)256 * plan.tiles;
     for (int pass = 0; pass < plan.passes; ++pass) {
         const int shift = 8 * pass;
-        radix_upsweep_kernel<<<plan.tiles, kThreads, 0, s>>>(keys[cur], plan.n, shift, plan.tiles, hist);
+        if (plan.rounds == 4)
+            radix_upsweep_kernel<4><<<plan.tiles, kThreads, 0, s>>>(keys[cur], plan.n, shift, plan.tiles, hist);
+        else
+            radix_upsweep_kernel<16><<<plan.tiles, kThreads, 0, s>>>(keys[cur], plan.n, shift, plan.tiles, hist);
         radix_scan_kernel<<<256, kThreads, 0, s>>>(hist, plan.tiles, totals);
-        radix_downsweep_kernel<<<plan.tiles, kThreads, 0, s>>>(keys[cur], perm[cur], keys[cur ^ 1], perm[cur ^ 1],
-                                                               plan.n, shift, plan.tiles, hist, totals);
+        if (plan.rounds == 4)
+            radix_downsweep_kernel<4><<<plan.tiles, kThreads, 0, s>>>(keys[cur], perm[cur], keys[cur ^ 1],
+                                                                      perm[cur ^ 1], plan.n, shift, plan.tiles, hist,
+                                                                      totals);
+        else
+            radix_downsweep_kernel<16><<<plan.tiles, kThreads, 0, s>>>(keys[cur], perm[cur], keys[cur ^ 1],
+                                                                       perm[cur ^ 1], plan.n, shift, plan.tiles, hist,
+                                                                       totals);
         cur ^= 1;
     }
     return cur;
