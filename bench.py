@@ -324,7 +324,8 @@ def gpu_arm(args) -> None:
         issue = {"kernel": dominant, "warp_instructions_per_launch": inst,
                  "achieved": inst / (launch_ms / 1000.0), "peak": peak_issue, "unit": "warp instructions/s",
                  "frac": inst / (launch_ms / 1000.0) / peak_issue,
-                 "source": "ncu smsp__inst_executed.sum of one launch after 50 frames, scaled by list length"}
+                 "source": "ncu smsp__inst_executed.sum of one launch after 50 frames (256-thread blocks, plain "
+                           "thread map), scaled by list length"}
     # ---- the other arithmetic mode, same scene state, its own block sizes ----
     other_line = None
     if not args.no_other_mode:
