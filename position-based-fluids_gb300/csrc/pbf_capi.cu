@@ -1350,6 +1350,7 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
         for (int q = 0; q < 4; ++q) { solverMs[bal][q] = 1e30f; solverBlock[bal][q] = 256; }
     ctx->stageTiming = true;
     for (int trial = 0; trial < 16; ++trial) {
+        // block size x friends algorithm x balanced thread map
         const int cand = candidates[trial % 4], algo = (trial / 4) & 1, bal = trial / 8;
         ctx->shape = pbf::LaunchShape{cand, cand, cand, cand, cand, algo, bal};
         ctx->stageNames.clear();

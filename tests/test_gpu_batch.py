@@ -58,7 +58,7 @@ def test_autotune_keeps_results_and_state(pbf_mod, cuda_device):
         b.Step(2)
         for x, y in zip(a.read_state(), b.read_state()):
             assert _same(x, y)
-        b.set_launch_shape([96, 160, 224, 288, 352, 1 - blocks[5], 1 - blocks[6]])  # the other algorithm, balance
+        b.set_launch_shape([96, 160, 224, 288, 352, 1 - blocks[5], 1 - blocks[6]])  # the other algorithm and map
         b.Step(1)
         a.Step(1)
         for x, y in zip(a.read_state(), b.read_state()):

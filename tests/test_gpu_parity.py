@@ -55,8 +55,8 @@ def assert_same(name, got, want):
 def run_gpu(pbf, params, pos, vel, substeps, device, graph=True, friends=True, algorithm=None):
     with pbf.Simulation.create(params, pos, vel, device=device) as sim:
         sim.use_graph(graph)
-        if algorithm is not None:  # friends algorithm, and the balanced map with the warp one
-            sim.set_launch_shape(sim.launch_shape()[:5] + [algorithm, algorithm])
+        if algorithm is not None:  # friends algorithm; the balanced map with the warp one
+            sim.set_launch_shape(sim.launch_shape()[:5] + [algorithm, 1 if algorithm == 1 else 0])
         sim.Step(substeps)
         p, v, pr = sim.read_state()
         counts, lst = sim.read_friends() if friends else (None, None)
