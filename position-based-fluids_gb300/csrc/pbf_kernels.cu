@@ -146,6 +146,7 @@ __device__ __forceinline__ int circles_kept(uint64_t cnt, int C, int total, floa
 // formed from the three spread coordinates of each axis, and the circle is
 // read off precomputed r^2 thresholds (DevConsts::circT): the same integer
 // the sqrt / divide / cube / truncate sequence gives, without computing it.
+template <int U>
 __global__ void __launch_bounds__(kMaxBlock)
 build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const uint2* __restrict__ cells,
                      uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
@@ -175,15 +176,17 @@ build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, cons
         list[(size_t)(circ * P + (int)k) * n + i] = j;
         cnt += 1ull << (8 * circ);
     };
-    // candidates lo .. hi in order, two loads in flight
+    // candidates lo .. hi in order, U loads in flight
     auto scan = [&](uint32_t lo, uint32_t hi) {
         uint32_t j = lo;
-        for (; j + 1 <= hi; j += 2) {
-            const float4 p0 = __ldg(pred + j), p1 = __ldg(pred + j + 1);
-            consider(j, p0);
-            consider(j + 1, p1);
+        for (; j + (U - 1) <= hi; j += U) {
+            float4 p[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) p[u] = __ldg(pred + j + u);
+#pragma unroll
+            for (int u = 0; u < U; ++u) consider(j + u, p[u]);
         }
-        if (j <= hi) consider(j, __ldg(pred + j));
+        for (; j <= hi; ++j) consider(j, __ldg(pred + j));
     };
     for (int x = -1; x <= 1; ++x) {
         const uint32_t ex = x < 0 ? exm : (x > 0 ? exp_ : ex0);
@@ -698,7 +701,7 @@ void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream
 
 void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
                           uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s) {
-    auto k = algorithm == 1 ? build_friends_warp_kernel : build_friends_kernel;
+    auto k = algorithm == 1 ? build_friends_warp_kernel : build_friends_kernel<2>;
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, reinterpret_cast<const uint2*>(cells), list, meta, errorWord);
 }
 
