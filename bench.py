@@ -291,6 +291,13 @@ def gpu_arm(args) -> None:
     e2e_s = time.perf_counter() - t0
     e2e_value, _ = replica_rate(n * iters * sub * e2e_steps, e2e_s, dist, "cuda")
 
+    # ---- density error of the state after the timed frames ----
+    _, _, dpred = sim.read_state()
+    rel = np.abs(dpred[:, 3].astype(np.float64) / float(params.restDensity) - 1.0)
+    rel = rel[np.isfinite(rel)]
+    density_error = {"mean": float(rel.mean()), "p95": float(np.percentile(rel, 95)), "max": float(rel.max()),
+                     "note": "|rho / rho0 - 1| per particle, density of the last solver iteration"}
+
     # ---- per-stage device times (eager launches, events between stages) ----
     counts, _ = sim.read_friends(slots=1)
     nl, nd = float(counts[:, 0].mean()), float(counts[:, 1].mean())
@@ -385,6 +392,7 @@ def gpu_arm(args) -> None:
         **({"issue_roofline": issue} if issue else {}),
         "stage_ms_per_step": {k: round(v, 4) for k, v in sorted(stage_ms.items(), key=lambda kv: -kv[1])},
         "neighbours": {"density_pass": nl, "other_passes": nd},
+        "density_error": density_error,
         **({"other_mode": other_line} if other_line else {}),
         "clocks": clocks.summary(),
     }

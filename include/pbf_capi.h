@@ -58,6 +58,16 @@ int pbf_default_parameters(PbfParameters* out);
    boxclamp, zerodistanceguard and relaxedmath.  Returns the number of unknown keys through *unknown (may be NULL). */
 int pbf_load_parameters(const char* text, PbfParameters* inout, int* unknown);
 
+/* The scene keys of `.par` text (BlockDims, BlockOrigin, Jitter, Seed) into
+   *scene; PBF_ERR_INVALID without a BlockDims line.  pbf_load_parameters
+   accepts these keys silently. */
+int pbf_load_scene(const char* text, PbfScene* scene);
+
+/* The scene's nx*ny*nz particles (4 floats each, x fastest): lattice spacing
+   p->h * p->setupSpacing from blockOrigin, each coordinate jittered by
+   U(-jitter, jitter) from a 64-bit Mersenne Twister seeded with seed. */
+int pbf_scene_positions(const PbfParameters* p, const PbfScene* scene, float* pos);
+
 /* -------------------------------------------------------------- lifetime -- */
 
 /* Create a context on CUDA device `device`.
@@ -223,6 +233,11 @@ int pbf_read_friends(pbf_ctx* ctx, uint32_t* counts, uint32_t* list, int list_sl
 int pbf_enable_stage_timing(pbf_ctx* ctx, int enable);
 int pbf_stage_timings(pbf_ctx* ctx, float* ms, int capacity, int* count,
                       char* names, size_t names_len);
+
+/* NVTX ranges (named as the trackers) around the stages of every substep
+   enqueued eagerly (stage timing on, or graphs off), for nsys / ncu
+   --nvtx-include.  Header-only NVTX: a no-op without a profiler attached. */
+int pbf_enable_nvtx(pbf_ctx* ctx, int enable);
 
 /* One performance tracker, the fields of the reference's
    PM_PERFORMANCE_TRACKER (src/OCLPerfMon.h) without the OpenCL event.

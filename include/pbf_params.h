@@ -105,6 +105,17 @@ typedef struct PbfCamera {
     int32_t width, height;   /* pixels, each at most 8192 */
 } PbfCamera;
 
+/* The initial block of a scenario file (`.par` keys BlockDims, BlockOrigin,
+   Jitter, Seed; the spacing is SmoothLen x SetupSpacing, as the reference's
+   CreateParticles spaces its lattice).  The reference's loader reports these
+   keys as unknown and skips them, so the files stay readable by it. */
+typedef struct PbfScene {
+    int32_t  blockDims[3];
+    float    blockOrigin[3];
+    float    jitter;
+    uint64_t seed;
+} PbfScene;
+
 /* Largest number of force planes. */
 #define PBF_MAX_FORCE_QUADS        64
 

@@ -88,7 +88,9 @@ extern "C" int pbf_load_parameters(const char* text, PbfParameters* p, int* unkn
         else if (key == "boxclamp") fields >> p->boxClamp;
         else if (key == "zerodistanceguard") fields >> p->zeroDistanceGuard;
         else if (key == "relaxedmath") fields >> p->relaxedMath;
-        else {
+        else if (key == "blockdims" || key == "blockorigin" || key == "jitter" || key == "seed") {
+            // scene keys (pbf_load_scene)
+        } else {
             std::cerr << "Unknown parameter " << key << std::endl << "Leaving it out." << std::endl;
             ++nUnknown;
         }
@@ -96,6 +98,38 @@ extern "C" int pbf_load_parameters(const char* text, PbfParameters* p, int* unkn
     apply_computed_fields(p);
     if (unknown) *unknown = nUnknown;
     return PBF_OK;
+}
+
+// The scene keys of a `.par` file: BlockDims nx ny nz, BlockOrigin x y z,
+// Jitter j, Seed s.  Other keys are left to pbf_load_parameters.
+extern "C" int pbf_load_scene(const char* text, PbfScene* scene) {
+    if (!text || !scene) return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_load_scene: NULL argument");
+    std::memset(scene, 0, sizeof(*scene));
+    std::istringstream in{std::string(text)};
+    std::string line, key;
+    bool dims = false;
+    while (std::getline(in, line)) {
+        line.erase(std::find(line.begin(), line.end(), '#'), line.end());
+        std::transform(line.begin(), line.end(), line.begin(), [](unsigned char c) { return (char)std::tolower(c); });
+        std::istringstream fields(line);
+        if (!(fields >> key)) continue;
+        if (key == "blockdims") dims = (bool)(fields >> scene->blockDims[0] >> scene->blockDims[1] >> scene->blockDims[2]);
+        else if (key == "blockorigin") fields >> scene->blockOrigin[0] >> scene->blockOrigin[1] >> scene->blockOrigin[2];
+        else if (key == "jitter") fields >> scene->jitter;
+        else if (key == "seed") fields >> scene->seed;
+    }
+    if (!dims || scene->blockDims[0] < 1 || scene->blockDims[1] < 1 || scene->blockDims[2] < 1)
+        return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_load_scene: no valid BlockDims line");
+    return PBF_OK;
+}
+
+// The scene's particles: a BlockDims lattice at spacing SmoothLen x
+// SetupSpacing (the reference's spacing, src/Simulation.cpp:77) from
+// BlockOrigin, jittered by U(-Jitter, Jitter) from Seed (pbf_scene_block).
+extern "C" int pbf_scene_positions(const PbfParameters* p, const PbfScene* s, float* pos) {
+    if (!p || !s || !pos) return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_scene_positions: NULL argument");
+    return pbf_scene_block(s->blockDims[0], s->blockDims[1], s->blockDims[2], p->h * p->setupSpacing,
+                           s->blockOrigin[0], s->blockOrigin[1], s->blockOrigin[2], s->jitter, s->seed, pos);
 }
 
 // Simulation::CreateParticles (src/Simulation.cpp:71-101): a cube of

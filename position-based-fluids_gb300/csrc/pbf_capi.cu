@@ -16,6 +16,7 @@
 // captured CUDA graph replays every substep.
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -82,6 +83,7 @@ struct pbf_ctx {
     uint64_t launches = 0;
 
     bool stageTiming = false;
+    bool nvtx = false;                       // NVTX ranges around the stages of eager substeps
     std::vector<std::string> stageNames;
     std::vector<float> stageMs;
     // per-launch trackers in the reference's naming (OCLPerfMon), EMA 0.5
@@ -403,7 +405,18 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     const int P = ctx->curPos, V = ctx->curVel;
     const bool paused = ctx->paused != 0;
     uint64_t launched = 0;
-    auto mark = [&](const char* name, int iteration = -1) { return clock ? clock->stage(name, iteration) : PBF_OK; };
+    bool rangeOpen = false;
+    auto mark = [&](const char* name, int iteration = -1) {
+        if (ctx->nvtx) {  // one range per stage, named as its tracker
+            if (rangeOpen) nvtxRangePop();
+            char label[64];
+            if (iteration >= 0) std::snprintf(label, sizeof label, "%s_%d", name, iteration);
+            else std::snprintf(label, sizeof label, "%s", name);
+            nvtxRangePushA(label);
+            rangeOpen = true;
+        }
+        return clock ? clock->stage(name, iteration) : PBF_OK;
+    };
 
     mark("predictPositions");
     const pbf::Batch b = batch_of(ctx);
@@ -466,6 +479,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     mark("applyVorticity");
     pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, ls.vorticity, ls.balance, s);
     launched += 3;
+    if (rangeOpen) nvtxRangePop();
     PBF_CUDA(ctx, cudaGetLastError());
     ctx->curPos = sortedPos ^ 1;
     ctx->curPred = a;
@@ -1225,6 +1239,12 @@ int pbf_enable_stage_timing(pbf_ctx* ctx, int enable) {
         if (!ctx->timingAnchor) PBF_CUDA(ctx, cudaEventCreate(&ctx->timingAnchor));
         PBF_CUDA(ctx, cudaEventRecord(ctx->timingAnchor, ctx->stream));
     }
+    return PBF_OK;
+}
+
+int pbf_enable_nvtx(pbf_ctx* ctx, int enable) {
+    if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    ctx->nvtx = enable != 0;
     return PBF_OK;
 }
 

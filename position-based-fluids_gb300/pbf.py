@@ -145,6 +145,9 @@ def library() -> ctypes.CDLL:
         "pbf_set_force_quads": [c_void_p, c_void_p, c_int],
         "pbf_set_wave_position": [c_void_p, c_float],
         "pbf_perf_trackers": [c_void_p, c_void_p, c_int, POINTER(c_int)],
+        "pbf_enable_nvtx": [c_void_p, c_int],
+        "pbf_load_scene": [c_char_p, c_void_p],
+        "pbf_scene_positions": [P, c_void_p, f32p],
         "pbf_render_camera": [c_void_p, c_void_p, c_void_p, c_float, c_int, c_int, c_float, c_void_p],
         "pbf_render_frame": [c_void_p, c_void_p, c_int],
         "pbf_render_read": [c_void_p, c_int, f32p],
@@ -415,6 +418,9 @@ class Simulation:
         _check(self.lib.pbf_render_read(self._ctx, int(which), _f32(img)), self._ctx)
         return img
 
+    def enable_nvtx(self, on: bool = True) -> None:
+        _check(self.lib.pbf_enable_nvtx(self._ctx, int(on)), self._ctx)
+
     def perf_trackers(self) -> list:
         """[(eventName, time_start ns, time_end ns, total_time ms, last_time ms)] in order of first use."""
         count = c_int(0)
@@ -498,24 +504,40 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_read_ids", "pbf_rollout_forward", "pbf_rollout_backward", "pbf_set_force_quads",
         "pbf_set_wave_position", "pbf_wave_position", "pbf_save_state", "pbf_load_state",
         "pbf_perf_trackers", "pbf_perf_export_json", "pbf_render_camera", "pbf_render_frame", "pbf_render_read",
-        "pbf_write_state_async", "pbf_read_state_async",
+        "pbf_write_state_async", "pbf_read_state_async", "pbf_enable_nvtx", "pbf_load_scene", "pbf_scene_positions",
     ])
 
 
 # Dam-break scenes: scenario file + the block the particles start in.
-SCENES = {
-    "dam_break_32k": dict(par="dam_break_32k", block=(32, 32, 32), spacing=0.05, origin=(0.025, 0.025, 0.025),
-                          jitter=0.005, seed=20240601),
-    "dam_break_1m": dict(par="dam_break_1m", block=(128, 64, 128), spacing=0.05, origin=(0.025, 0.025, 0.025),
-                         jitter=0.005, seed=20240601),
-}
+SCENES = ("dam_break_32k", "dam_break_1m", "dam_break_32k_literal")
+
+
+class PbfScene(ctypes.Structure):
+    """PbfScene (include/pbf_params.h): a scenario file's initial block."""
+    _fields_ = [("blockDims", ctypes.c_int32 * 3), ("blockOrigin", c_float * 3), ("jitter", c_float),
+                ("seed", c_uint64)]
+
+
+def load_scene(text: str) -> PbfScene:
+    """pbf_load_scene: the BlockDims / BlockOrigin / Jitter / Seed keys."""
+    s = PbfScene()
+    _check(library().pbf_load_scene(text.encode(), ctypes.byref(s)))
+    return s
+
+
+def scene_positions(params: PbfParameters, scene: PbfScene) -> np.ndarray:
+    n = scene.blockDims[0] * scene.blockDims[1] * scene.blockDims[2]
+    out = np.zeros((n, 4), np.float32)
+    _check(library().pbf_scene_positions(ctypes.byref(params), ctypes.byref(scene), _f32(out)))
+    return out
 
 
 def make_scene(name: str):
-    """(params, pos[N,4], vel[N,4]) of a bundled dam-break scene."""
-    spec = SCENES[name]
-    params = load_scenario(spec["par"])
-    pos = scene_block(*spec["block"], spec["spacing"], spec["origin"], spec["jitter"], spec["seed"])
+    """(params, pos[N,4], vel[N,4]) of a bundled scenario file: its
+    parameters and its initial block (BlockDims, BlockOrigin, Jitter, Seed)."""
+    text = (PKG / "scenarios" / f"{name}.par").read_text()
+    params = load_parameters(text)
+    pos = scene_positions(params, load_scene(text))
     if pos.shape[0] != params.particleCount:
         raise ValueError(f"scene {name}: block holds {pos.shape[0]} particles, .par says {params.particleCount}")
     return params, pos, np.zeros_like(pos)

@@ -118,3 +118,20 @@ def test_wave_position_follows_the_runner_formula(pbf_mod):
         want = (1 - math.cos(2 * math.pi * math.fmod(0.7 * float(np.float32(t)), 1.0) ** 1.5)) * \
             0.2 * (p.xMax - p.xMin) / 2
         assert abs(pbf_mod.wave_position(p, t) - want) <= 1e-6 * max(1.0, abs(want))
+
+
+def test_scene_keys(pbf_mod):
+    """BlockDims / BlockOrigin / Jitter / Seed: read by pbf_load_scene, skipped
+    silently by the parameter loader, and the bundled scenes come from them."""
+    text = "SmoothLen 0.1\nSetupSpacing 0.5\nBlockDims 4 3 2\nBlockOrigin 0.1 0.2 0.3\nJitter 0.001\nSeed 7\n"
+    s = pbf_mod.load_scene(text)
+    assert list(s.blockDims) == [4, 3, 2] and s.seed == 7
+    assert abs(s.jitter - 0.001) < 1e-9 and abs(s.blockOrigin[2] - 0.3) < 1e-7
+    params = pbf_mod.load_parameters(text)
+    pos = pbf_mod.scene_positions(params, s)
+    want = pbf_mod.scene_block(4, 3, 2, 0.05, (0.1, 0.2, 0.3), 0.001, 7)
+    assert np.array_equal(pos, want)
+    with pytest.raises(pbf_mod.PbfError):
+        pbf_mod.load_scene("SmoothLen 0.1\n")
+    p, pos32, _ = pbf_mod.make_scene("dam_break_32k")
+    assert pos32.shape == (32768, 4) and p.particleCount == 32768
