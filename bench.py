@@ -437,6 +437,7 @@ def sweep(args) -> None:
             for _ in range(args.sweep_warmup):
                 sim.step_async(sub)
             sim.synchronize()
+            blocks = sim.autotune(trial_substeps=2) if not args.no_autotune else sim.launch_shape()
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             ev0.record(stream)
             for _ in range(args.sweep_steps):
@@ -469,7 +470,9 @@ def sweep(args) -> None:
             line = {"sweep": "double_dam_break", "particles": n, "iterations": iters,
                     "value": n * iters * sub / (frame_ms / 1e3), "unit": UNIT, "ms_per_step": frame_ms,
                     "steps": args.sweep_steps, "warmup": args.sweep_warmup, "neighbours": {"density_pass": nl,
-                    "other_passes": nd}, "groups": groups, "peak_gbs": peak, "peak_source": peak_kind}
+                    "other_passes": nd}, "groups": groups, "peak_gbs": peak, "peak_source": peak_kind,
+                    "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm",
+                                        "balance"], blocks))}
             print(json.dumps(line), flush=True)
 
 
