@@ -7,9 +7,9 @@
 // included once, before the kernel sources, by the generated translation
 // unit oracle/_ref/ref_kernels.cpp.
 //
-// Work-items run one after another on the host: the driver sets the
+// Work-items run one after another on the host: ref_driver.inc sets the
 // work-item ids in `clref::wi` before each call.  barrier() is a no-op, which
-// is exact for every kernel the driver runs (each work-item of histogram /
+// is exact for every kernel ref_driver.inc runs (each work-item of histogram /
 // reorder touches only its own local-memory column); scanhistograms and
 // pastehistograms are not run through the shim.
 //

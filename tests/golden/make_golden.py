@@ -47,7 +47,7 @@ CASES = [
     ("circles3_iter2_odd", (17, 13, 11), {"friendsCircles": 3, "simIterations": 2}, 2),
     # larger kernel radius: more neighbours per particle
     ("wide_h_4k", (16, 16, 16), {"h": 0.13, "h_2": 0.13 * 0.13, "gridBufSize": 4096}, 1),
-    # the BASELINE solver constants: violent dynamics (velocities of tens of m/s)
+    # the benchmark's published solver constants: violent dynamics (velocities of tens of m/s)
     ("literal_32k_8sub", (32, 32, 32), {"base": "dam_break_32k_literal"}, 8),
 ]
 SEED = 20240601
