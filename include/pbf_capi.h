@@ -385,7 +385,9 @@ int pbf_render_read(pbf_ctx* ctx, int which, float* rgba);
    five neighbour kernels in the order friends, density (scaling), delta,
    viscosity, vorticity (multiples of 32 in [32, 512]), then the friends
    algorithm (0: one thread scans the 27 cells per particle; 1: a warp scans
-   the cells of each run of same-cell particles together), then the balance
+   the cells of each run of same-cell particles together; 2: a block stages
+   the 6x6x6-cell halo of a 4x4x4-cell brick in shared memory and its threads
+   scan from there, for power-of-two GridBufferSize >= 64, else 0), then the balance
    flag (1: the four solver passes hand each block's particles to its threads
    in decreasing order of friend count, so warps walk lists of similar
    length).  Results do not depend on any of them. */
@@ -394,7 +396,7 @@ int pbf_get_launch_shape(pbf_ctx* ctx, int* blocks);
 int pbf_set_launch_shape(pbf_ctx* ctx, const int* blocks);
 
 /* Time `trial_substeps` substeps from the current state for each candidate
-   block size (64, 128, 256, 512), both friends algorithms and both balance
+   block size (64, 128, 256, 512), the three friends algorithms and both balance
    settings, keep the fastest per kernel (the balance setting by the sum of
    the solver passes), restore the state, and report the choice through
    blocks_out (PBF_LAUNCH_SHAPE_FIELDS ints, may be NULL). */

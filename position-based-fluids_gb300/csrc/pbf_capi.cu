@@ -300,7 +300,9 @@ int validate(pbf_ctx* ctx, const PbfParameters& p) {
 
 bool is_batch(const pbf_ctx* ctx) { return !ctx->sceneParams.empty(); }
 
-pbf::Batch batch_of(const pbf_ctx* ctx) { return pbf::Batch{ctx->scenes, ctx->sceneOf}; }
+pbf::Batch batch_of(const pbf_ctx* ctx) {
+    return pbf::Batch{ctx->scenes, ctx->sceneOf, ctx->scenes ? (int)ctx->sceneParams.size() : 0};
+}
 
 // Scenes of a batch share every parameter but the particle count, the box,
 // the gravity and the XSPH factor.
@@ -1313,7 +1315,7 @@ int pbf_set_launch_shape(pbf_ctx* ctx, const int* blocks) {
     for (int k = 0; k < 5; ++k)
         if (blocks[k] < 32 || blocks[k] > pbf::kMaxBlock || blocks[k] % 32)
             return fail(ctx, PBF_ERR_INVALID, "block sizes must be multiples of 32 in [32, 512]");
-    if (blocks[5] != 0 && blocks[5] != 1) return fail(ctx, PBF_ERR_INVALID, "the friends algorithm is 0 or 1");
+    if (blocks[5] < 0 || blocks[5] > 2) return fail(ctx, PBF_ERR_INVALID, "the friends algorithm is 0, 1 or 2");
     if (blocks[6] != 0 && blocks[6] != 1) return fail(ctx, PBF_ERR_INVALID, "the balance flag is 0 or 1");
     ctx->shape.friends = blocks[0]; ctx->shape.scaling = blocks[1]; ctx->shape.delta = blocks[2];
     ctx->shape.viscosity = blocks[3]; ctx->shape.vorticity = blocks[4]; ctx->shape.friendsAlgorithm = blocks[5];
@@ -1369,9 +1371,9 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
     for (int bal = 0; bal < 2; ++bal)
         for (int q = 0; q < 4; ++q) { solverMs[bal][q] = 1e30f; solverBlock[bal][q] = 256; }
     ctx->stageTiming = true;
-    for (int trial = 0; trial < 16; ++trial) {
-        // block size x friends algorithm x balanced thread map
-        const int cand = candidates[trial % 4], algo = (trial / 4) & 1, bal = trial / 8;
+    for (int trial = 0; trial < 24; ++trial) {
+        // block size x friends algorithm (3) x balanced thread map (2)
+        const int cand = candidates[trial % 4], algo = (trial / 4) % 3, bal = trial / 12;
         ctx->shape = pbf::LaunchShape{cand, cand, cand, cand, cand, algo, bal};
         ctx->stageNames.clear();
         ctx->stageMs.clear();

@@ -66,13 +66,15 @@ struct SceneParams {
 struct Batch {
     const SceneParams* scenes;
     const uint16_t* sceneOf;
+    int nscenes = 0;
 };
 SceneParams make_scene_params(const PbfParameters& p, uint32_t keyBase);
 
 // Threads per block of the kernels whose block size the autotuner chooses.
 struct LaunchShape {
     int friends = 256, scaling = 256, delta = 256, viscosity = 256, vorticity = 256;
-    int friendsAlgorithm = 0;  // 0: one thread scans per particle; 1: warp-cooperative runs
+    int friendsAlgorithm = 0;  // 0: one thread scans per particle; 1: warp-cooperative runs;
+                               // 2: 4x4x4-cell bricks streamed through shared memory
     int balance = 0;           // solver passes: threads take the block's particles by friend count
 };
 constexpr int kMaxBlock = 512;

@@ -138,45 +138,64 @@ __device__ __forceinline__ int circles_kept(uint64_t cnt, int C, int total, floa
     return kept;
 }
 
-// build_friends_list.cl:29-102: one scan of the 27 neighbour cells in the
-// reference's order (x, then y, then z offsets; particles of a cell in sorted
-// order), self excluded, r^2 < h^2, binned into circles by
-// min(int(adj^3 * C), C-1) with adj = max(0, (r - 0.3h) / 0.7h), at most
-// perCircle per circle (later ones are dropped, :79-83).  The 27 hashes are
-// formed from the three spread coordinates of each axis, and the circle is
-// read off precomputed r^2 thresholds (DevConsts::circT): the same integer
-// the sqrt / divide / cube / truncate sequence gives, without computing it.
-template <int U>
-__global__ void __launch_bounds__(kMaxBlock)
-build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const uint2* __restrict__ cells,
-                     uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = c.n;
-    if (i >= n) return;
-    const float4 pi = pred[i];
-    const int cx = __float2int_rz(pi.x / c.h), cy = __float2int_rz(pi.y / c.h), cz = __float2int_rz(pi.z / c.h);
-    const int C = c.circles, P = c.perCircle;
-    const bool pow2 = (c.grid & (c.grid - 1)) == 0;
-    const uint32_t mask = c.grid - 1;
-    const uint32_t exm = expand_bits(cx - 1), ex0 = expand_bits(cx), exp_ = expand_bits(cx + 1);
-    const uint32_t eym = expand_bits(cy - 1) << 1, ey0 = expand_bits(cy) << 1, eyp = expand_bits(cy + 1) << 1;
-    const uint32_t ezm = expand_bits(cz - 1) << 2, ez0 = expand_bits(cz) << 2, ezp = expand_bits(cz + 1) << 2;
-    const uint32_t base = key_base(b, i);
-    const uint32_t selfHash = pow2 ? ((ex0 | ey0 | ez0) & mask) : ((ex0 | ey0 | ez0) % c.grid);
+// One particle's friend circles as the candidates arrive (build_friends_list.cl:
+// 58-95): r^2 < h^2, binned into circles by min(int(adj^3 * C), C-1) with
+// adj = max(0, (r - 0.3h) / 0.7h), at most perCircle per circle (later ones
+// are dropped, :79-83).  The circle is read off precomputed r^2 thresholds
+// (DevConsts::circT): the same integer the sqrt / divide / cube / truncate
+// sequence gives, without computing it.
+struct FriendCircles {
+    const DevConsts& c;
+    uint32_t* list;
+    int n, i;
+    float4 pi;
     uint64_t cnt = 0;  // 8 circles x 8-bit counters
-    auto consider = [&](uint32_t j, const float4 pj) {
+    __device__ __forceinline__ FriendCircles(const DevConsts& cc, uint32_t* l, int i_, float4 p)
+        : c(cc), list(l), n(cc.n), i(i_), pi(p) {}
+    __device__ __forceinline__ void consider(uint32_t j, const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = dot3(rx, ry, rz, rx, ry, rz);
         if (r2 >= c.h2) return;
         // thresholds past C-1 are +inf, so only the first C-1 decide
         int circ = (r2 >= c.circT[0]) + (r2 >= c.circT[1]) + (r2 >= c.circT[2]) + (r2 >= c.circT[3]);
-        if (C > 5) circ += (r2 >= c.circT[4]) + (r2 >= c.circT[5]) + (r2 >= c.circT[6]);
+        if (c.circles > 5) circ += (r2 >= c.circT[4]) + (r2 >= c.circT[5]) + (r2 >= c.circT[6]);
         const uint32_t k = byte_of(cnt, circ);
-        if ((int)k >= P) return;
-        list[(size_t)(circ * P + (int)k) * n + i] = j;
+        if ((int)k >= c.perCircle) return;
+        list[(size_t)(circ * c.perCircle + (int)k) * n + i] = j;
         cnt += 1ull << (8 * circ);
-    };
-    // candidates lo .. hi in order, U loads in flight
+    }
+    __device__ __forceinline__ void finish(uint2* meta) const {
+        const int C = c.circles;
+        int total = 0;
+        uint64_t mt = 0;
+        for (int k = 0; k < C; ++k) {
+            total += (int)byte_of(cnt, k);
+            mt |= (uint64_t)byte_of(cnt, k) << (7 * k);
+        }
+        mt |= (uint64_t)circles_kept(cnt, C, total, 0.6f) << 56;
+        mt |= (uint64_t)circles_kept(cnt, C, total, 0.5f) << 60;
+        meta[i] = make_uint2((uint32_t)mt, (uint32_t)(mt >> 32));
+    }
+};
+
+// build_friends_list.cl:29-102 for particle i: one scan of the 27 neighbour
+// cells in the reference's order (x, then y, then z offsets; particles of a
+// cell in sorted order), self excluded, candidates read through L1 with U
+// loads in flight.  The 27 hashes are formed from the three spread
+// coordinates of each axis.
+template <int U>
+__device__ __forceinline__ void friends_scan_global(const DevConsts& c, uint32_t base, const float4* __restrict__ pred,
+                                                   const uint2* __restrict__ cells, int* __restrict__ err,
+                                                   FriendCircles& fc) {
+    const int i = fc.i, n = c.n;
+    const float4 pi = fc.pi;
+    const int cx = __float2int_rz(pi.x / c.h), cy = __float2int_rz(pi.y / c.h), cz = __float2int_rz(pi.z / c.h);
+    const bool pow2 = (c.grid & (c.grid - 1)) == 0;
+    const uint32_t mask = c.grid - 1;
+    const uint32_t exm = expand_bits(cx - 1), ex0 = expand_bits(cx), exp_ = expand_bits(cx + 1);
+    const uint32_t eym = expand_bits(cy - 1) << 1, ey0 = expand_bits(cy) << 1, eyp = expand_bits(cy + 1) << 1;
+    const uint32_t ezm = expand_bits(cz - 1) << 2, ez0 = expand_bits(cz) << 2, ezp = expand_bits(cz + 1) << 2;
+    const uint32_t selfHash = pow2 ? ((ex0 | ey0 | ez0) & mask) : ((ex0 | ey0 | ez0) % c.grid);
     auto scan = [&](uint32_t lo, uint32_t hi) {
         uint32_t j = lo;
         for (; j + (U - 1) <= hi; j += U) {
@@ -184,9 +203,9 @@ build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, cons
 #pragma unroll
             for (int u = 0; u < U; ++u) p[u] = __ldg(pred + j + u);
 #pragma unroll
-            for (int u = 0; u < U; ++u) consider(j + u, p[u]);
+            for (int u = 0; u < U; ++u) fc.consider(j + u, p[u]);
         }
-        for (; j <= hi; ++j) consider(j, __ldg(pred + j));
+        for (; j <= hi; ++j) fc.consider(j, __ldg(pred + j));
     };
     for (int x = -1; x <= 1; ++x) {
         const uint32_t ex = x < 0 ? exm : (x > 0 ? exp_ : ex0);
@@ -209,15 +228,154 @@ build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, cons
             }
         }
     }
-    int total = 0;
-    uint64_t mt = 0;
-    for (int k = 0; k < C; ++k) {
-        total += (int)byte_of(cnt, k);
-        mt |= (uint64_t)byte_of(cnt, k) << (7 * k);
+}
+
+// One thread per particle, candidates through L1.
+template <int U>
+__global__ void __launch_bounds__(kMaxBlock)
+build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const uint2* __restrict__ cells,
+                     uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    FriendCircles fc(c, list, i, pred[i]);
+    friends_scan_global<U>(c, key_base(b, i), pred, cells, err, fc);
+    fc.finish(meta);
+}
+
+// The same lists with the candidates streamed through shared memory, one
+// block per brick of B x B x B cells (B^3 consecutive Morton numbers, so the
+// brick's particles are one range of the sorted order).  The block stages the
+// brick's (B+2)^3 halo of cells into shared memory with coalesced float4
+// loads (every particle's 27 neighbour cells lie in it), then each thread
+// scans its particle's 27 cells from there in the reference's order.  A
+// particle whose cell is not the brick's (a key that aliases through the hash
+// modulo), or a halo too large for the buffer, takes the per-particle scan
+// through L1.  Needs a power-of-two GridBufferSize of at least B^3.
+template <int B> struct BrickShape;
+template <> struct BrickShape<4> { static constexpr int threads = 256, capacity = 2816; };  // 44 KB of float4
+
+__device__ __forceinline__ uint32_t compact_bits(uint32_t x) {
+    x &= 0x09249249u;
+    x = (x ^ (x >> 2)) & 0x030C30C3u;
+    x = (x ^ (x >> 4)) & 0x0300F00Fu;
+    x = (x ^ (x >> 8)) & 0x030000FFu;
+    x = (x ^ (x >> 16)) & 0x000003FFu;
+    return x;
+}
+
+template <int B>
+__global__ void __launch_bounds__(BrickShape<B>::threads)
+build_friends_brick_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* __restrict__ cells,
+                           uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
+    constexpr int T = BrickShape<B>::threads, kCap = BrickShape<B>::capacity;
+    constexpr int E = B + 2, kHalo = E * E * E, kCodes = B * B * B, kPerLane = (kHalo + 31) / 32;
+    __shared__ uint32_t hStart[kHalo], hCount[kHalo], hOff[kHalo];
+    __shared__ float4 staged[kCap];
+    __shared__ uint32_t firstP, lastP, haloTotal;
+    const int t = threadIdx.x, n = c.n;
+    const uint32_t key0 = blockIdx.x * (uint32_t)kCodes;   // first key of the brick
+    const uint32_t base = (key0 / c.grid) * c.grid;        // the scene's key offset
+    const uint32_t m0 = key0 - base;                       // its Morton number
+    const int bx = (int)compact_bits(m0), by = (int)compact_bits(m0 >> 1), bz = (int)compact_bits(m0 >> 2);
+    if (t == 0) { firstP = 0xFFFFFFFFu; lastP = 0u; }
+    __syncthreads();
+    for (int q = t; q < kCodes; q += T) {  // the brick's particle range
+        const uint2 r = cells[key0 + q];
+        if (r.x != kEmpty) {
+            atomicMin(&firstP, r.x);
+            atomicMax(&lastP, min(r.y, (uint32_t)(n - 1)));
+        }
     }
-    mt |= (uint64_t)circles_kept(cnt, C, total, 0.6f) << 56;
-    mt |= (uint64_t)circles_kept(cnt, C, total, 0.5f) << 60;
-    meta[i] = make_uint2((uint32_t)mt, (uint32_t)(mt >> 32));
+    const uint32_t mask = c.grid - 1;
+    for (int h = t; h < kHalo; h += T) {
+        const int hx = bx - 1 + h / (E * E), hy = by - 1 + (h / E) % E, hz = bz - 1 + h % E;
+        const uint32_t m = expand_bits(hx) | (expand_bits(hy) << 1) | (expand_bits(hz) << 2);
+        const uint2 range = cells[base + (m & mask)];
+        uint32_t count = 0;
+        if (range.x != kEmpty) {
+            const uint32_t last = min(range.y, (uint32_t)(n - 1));
+            if (range.x <= last) count = last - range.x + 1u;
+            else atomicOr(err, 1);
+        }
+        hStart[h] = range.x;
+        hCount[h] = count;
+    }
+    __syncthreads();
+    if (firstP == 0xFFFFFFFFu) return;  // an empty brick
+    if (t < 32) {  // exclusive scan of the halo counts
+        uint32_t v[kPerLane], s = 0;
+#pragma unroll
+        for (int k = 0; k < kPerLane; ++k) {
+            const int h = kPerLane * t + k;
+            v[k] = h < kHalo ? hCount[h] : 0u;
+            s += v[k];
+        }
+        uint32_t incl = s;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (t >= d) incl += u;
+        }
+        uint32_t run = incl - s;
+#pragma unroll
+        for (int k = 0; k < kPerLane; ++k) {
+            const int h = kPerLane * t + k;
+            if (h < kHalo) hOff[h] = run;
+            run += v[k];
+        }
+        if (t == 31) haloTotal = incl;
+    }
+    __syncthreads();
+    const uint32_t total = haloTotal;
+    const bool useSmem = total <= (uint32_t)kCap;
+    if (useSmem) {
+        for (uint32_t e = t; e < total; e += T) {
+            int lo = 0;  // the halo cell holding staged entry e: the last with hOff <= e
+#pragma unroll
+            for (int s = 128; s > 0; s >>= 1)
+                if (lo + s < kHalo && hOff[lo + s] <= e) lo += s;
+            while (lo < kHalo - 1 && (hCount[lo] == 0 || hOff[lo] + hCount[lo] <= e)) ++lo;
+            staged[e] = pred[hStart[lo] + (e - hOff[lo])];
+        }
+    }
+    __syncthreads();
+    for (uint32_t p = firstP + t; p <= lastP; p += T) {
+        const int i = (int)p;
+        FriendCircles fc(c, list, i, pred[i]);
+        const int cx = __float2int_rz(fc.pi.x / c.h), cy = __float2int_rz(fc.pi.y / c.h), cz = __float2int_rz(fc.pi.z / c.h);
+        const int lx = cx - bx, ly = cy - by, lz = cz - bz;
+        if (useSmem && (unsigned)lx < (unsigned)B && (unsigned)ly < (unsigned)B && (unsigned)lz < (unsigned)B) {
+            // staged entries [a, b) of one cell, candidates st + (k - off), two in flight, self skipped
+            auto scanStaged = [&](uint32_t a, uint32_t b, uint32_t jOfA) {
+                uint32_t k = a;
+                for (; k + 1 < b; k += 2) {
+                    const float4 p0 = staged[k], p1 = staged[k + 1];
+                    fc.consider(jOfA + (k - a), p0);
+                    fc.consider(jOfA + (k + 1 - a), p1);
+                }
+                if (k < b) fc.consider(jOfA + (k - a), staged[k]);
+            };
+#pragma unroll 1
+            for (int x = 0; x < 3; ++x)
+#pragma unroll 1
+                for (int y = 0; y < 3; ++y)
+#pragma unroll
+                    for (int z = 0; z < 3; ++z) {
+                        const int h = (lx + x) * (E * E) + (ly + y) * E + (lz + z);
+                        const uint32_t cnt = hCount[h], off = hOff[h], st = hStart[h];
+                        if ((uint32_t)i - st < cnt) {  // the particle's own range: skip itself
+                            const uint32_t self = off + ((uint32_t)i - st);
+                            scanStaged(off, self, st);
+                            scanStaged(self + 1, off + cnt, (uint32_t)i + 1);
+                        } else {
+                            scanStaged(off, off + cnt, st);
+                        }
+                    }
+        } else {
+            friends_scan_global<2>(c, base, pred, cells, err, fc);
+        }
+        fc.finish(meta);
+    }
 }
 
 // The same lists, built warp-cooperatively.  A warp takes its 32 particles
@@ -701,6 +859,14 @@ void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream
 
 void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
                           uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s) {
+    const bool pow2 = (c.grid & (c.grid - 1)) == 0;
+    const uint32_t keys = c.grid * (uint32_t)(b.scenes ? b.nscenes : 1);
+    const uint2* cellPairs = reinterpret_cast<const uint2*>(cells);
+    if (algorithm == 2 && pow2 && c.grid >= 64) {  // one block per 4x4x4-cell brick over all scenes
+        build_friends_brick_kernel<4><<<keys / 64u, BrickShape<4>::threads, 0, s>>>(c, pred, cellPairs, list, meta,
+                                                                                 errorWord);
+        return;
+    }
     auto k = algorithm == 1 ? build_friends_warp_kernel : build_friends_kernel<2>;
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, reinterpret_cast<const uint2*>(cells), list, meta, errorWord);
 }

@@ -114,7 +114,7 @@ def test_sort_at_full_scale_properties(pbf_mod, oracle_mod, cuda_device):
 MANIFEST = json.loads((GOLDEN / "golden.json").read_text())
 
 
-@pytest.mark.parametrize("algorithm", [0, 1], ids=["scan", "warp"])
+@pytest.mark.parametrize("algorithm", [0, 1, 2], ids=["scan", "warp", "brick"])
 @pytest.mark.parametrize("case", MANIFEST["cases"], ids=[c["name"] for c in MANIFEST["cases"]])
 def test_gpu_matches_reference_kernel_digests(case, algorithm, pbf_mod, cuda_device):
     """Outputs of the reference's own kernels (tests/golden) reproduced on the GPU."""
@@ -139,7 +139,7 @@ SUBSTEP_CASES = {
 }
 
 
-@pytest.mark.parametrize("algorithm", [0, 1], ids=["scan", "warp"])
+@pytest.mark.parametrize("algorithm", [0, 1, 2], ids=["scan", "warp", "brick"])
 @pytest.mark.parametrize("name", list(SUBSTEP_CASES))
 def test_substeps_bit_exact(name, algorithm, pbf_mod, oracle_mod, cuda_device):
     """Both friends algorithms (per-particle scan, warp-cooperative runs),
