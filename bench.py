@@ -652,6 +652,24 @@ def render(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def friends_compare(args) -> None:
+    """The friends build of the 1M dam break after the warm-up frames, once
+    with each algorithm from the same state (a short run to profile: one
+    substep with the shared-memory brick gather, one with the L1 scan)."""
+    import pbf
+    params, pos, vel = pbf.make_scene(SCENE)
+    sim = pbf.Simulation.create(params, pos, vel, device=0)
+    for _ in range(args.warmup):
+        sim.step_async(int(params.subSteps))
+    sim.synchronize()
+    for algorithm in (2, 0):
+        sim.set_launch_shape([256, 128, 128, 128, 128, algorithm, 0])
+        sim.Step(1)
+    sim.synchronize()
+    sim.close()
+    print(json.dumps({"friends_compare": "one substep each with friends algorithms 2 and 0", "warmup": args.warmup}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -676,6 +694,7 @@ def main() -> None:
     ap.add_argument("--batch-seq-steps", type=int, default=10)
     ap.add_argument("--rollout", action="store_true", help="differentiable rollout forward/backward instead")
     ap.add_argument("--render", action="store_true", help="headless renderer timings instead")
+    ap.add_argument("--friends-compare", action="store_true", help="one substep per friends algorithm (to profile)")
     ap.add_argument("--render-frames", type=int, default=20)
     ap.add_argument("--rollout-frames", type=int, default=60)
     ap.add_argument("--rollout-every", type=int, default=10)
@@ -687,6 +706,9 @@ def main() -> None:
         return
     if args.render:
         render(args)
+        return
+    if args.friends_compare:
+        friends_compare(args)
         return
     if args.batched:
         batched(args)
