@@ -78,6 +78,13 @@ typedef struct PbfParameters {
        multiply-adds.  Keys, sort, cell table and friend lists stay exact;
        one substep stays within 1e-5 relative of the exact result. */
     int          relaxedMath;
+    /* 0: the reference's neighbour sets: the density pass keeps the friend
+       circles up to 60 % of the friends, the other passes up to 50 %
+       (compute_scaling.cl:50, compute_delta.cl:100), and the density leaves
+       out the particle itself.  1: physically complete sets: every friend
+       circle in every pass, and the density includes the particle's own
+       W(0) term, added first. */
+    int          completeNeighbours;
 } PbfParameters;
 
 /* One force plane of the delta-p stage: BouncePointQuad's arguments

@@ -98,6 +98,7 @@ template <typename T> struct Consts {
     T dt, h, h2, minR, hMinusMinR, poly6, gradSpiky, poly6q, rho0, eps, K, visc, vort;
     T gx, gy, gz, lo[3], hi[3];
     int clamp, guard;
+    int complete;  // completeNeighbours: every circle in every pass, self in the density
     int circles, perCircle;
     uint32_t grid;
 };
@@ -124,6 +125,7 @@ template <typename T> Consts<T> make_consts(const PbfParameters& p) {
     c.hi[0] = p.xMax; c.hi[1] = p.yMax; c.hi[2] = p.zMax;
     c.clamp = p.boxClamp;
     c.guard = p.zeroDistanceGuard;
+    c.complete = p.completeNeighbours;
     c.circles = (int)p.friendsCircles; c.perCircle = (int)p.particlesPerCircle;
     c.grid = p.gridBufSize;
     return c;
@@ -296,9 +298,10 @@ template <typename T> void compute_scaling(State<T>& s, const Consts<T>& c) {
         const int32_t* cnt = &s.fcount[(size_t)i * C];
         const int32_t* lst = &s.friends[(size_t)i * C * P];
         V3<T> pi = xyz(s.pred[i]);
-        T density_sum = 0, grad_sum_k = 0;
+        // complete neighbour sets count the particle itself first: d = h^2 - 0
+        T density_sum = c.complete ? c.h2 * c.h2 * c.h2 : (T)0, grad_sum_k = 0;
         V3<T> grad_sum_k_i = {0, 0, 0};
-        int kept = circles_kept(cnt, C, 0.6f);
+        int kept = (c.complete ? C : circles_kept(cnt, C, 0.6f));
         for (int k = 0; k < kept; ++k)
             for (int f = 0; f < cnt[k]; ++f) {
                 V3<T> r = sub(pi, xyz(s.pred[lst[k * P + f]]));
@@ -384,7 +387,7 @@ template <typename T> void compute_delta(State<T>& s, const Consts<T>& c, uint8_
         const int32_t* lst = &s.friends[(size_t)i * C * P];
         V4<T> pi = s.predP[i];
         V3<T> sum = {0, 0, 0};
-        int kept = circles_kept(cnt, C, 0.5f);
+        int kept = (c.complete ? C : circles_kept(cnt, C, 0.5f));
         for (int k = 0; k < kept; ++k)
             for (int f = 0; f < cnt[k]; ++f) {
                 V4<T> pj = s.predP[lst[k * P + f]];
@@ -454,7 +457,7 @@ template <typename T> void apply_viscosity(State<T>& s, const Consts<T>& c) {
         const int32_t* lst = &s.friends[(size_t)i * C * P];
         V4<T> pi = s.pred[i], vi = vold[i];
         V3<T> vs = {0, 0, 0}, om = {0, 0, 0};
-        int kept = circles_kept(cnt, C, 0.5f);
+        int kept = (c.complete ? C : circles_kept(cnt, C, 0.5f));
         for (int k = 0; k < kept; ++k)
             for (int f = 0; f < cnt[k]; ++f) {
                 int j = lst[k * P + f];
@@ -490,7 +493,7 @@ template <typename T> void apply_vorticity(State<T>& s, const Consts<T>& c) {
         const int32_t* lst = &s.friends[(size_t)i * C * P];
         V4<T> pi = s.pred[i];
         V3<T> eta = {0, 0, 0};
-        int kept = circles_kept(cnt, C, 0.5f);
+        int kept = (c.complete ? C : circles_kept(cnt, C, 0.5f));
         for (int k = 0; k < kept; ++k)
             for (int f = 0; f < cnt[k]; ++f) {
                 int j = lst[k * P + f];
@@ -589,7 +592,7 @@ int run_steps(const PbfParameters* p, int n, T* pos, T* vel, T* pred, int subste
         for (int i = 0; i < n; ++i) {
             const int32_t* cnt = &s.fcount[(size_t)i * C];
             const int32_t* lst = &s.friends[(size_t)i * C * P];
-            int kl = circles_kept(cnt, C, 0.6f), kd = circles_kept(cnt, C, 0.5f);
+            int kl = (c.complete ? C : circles_kept(cnt, C, 0.6f)), kd = (c.complete ? C : circles_kept(cnt, C, 0.5f));
             uint32_t nl = 0, nd = 0, slot = 0;
             for (int k = 0; k < C; ++k) {
                 if (k < kl) nl += cnt[k];
@@ -640,6 +643,7 @@ template <typename T> struct Tape {
     std::vector<V4<T>> v2, omega;        // velocities before XSPH, vorticity
 };
 
+// The reference's truncation (rollouts use the reference's neighbour sets).
 inline void kept_circles(const int32_t* cnt, int C, int& keptL, int& keptD) {
     keptL = circles_kept(cnt, C, 0.6f);
     keptD = circles_kept(cnt, C, 0.5f);
@@ -1077,7 +1081,7 @@ int oracle_constants(const PbfParameters* p, float* poly6, float* grad_spiky, fl
 // the replay / gradient calls (free with oracle_rollout_free), NULL on error.
 void* oracle_rollout_record(const PbfParameters* p, int n, float* pos, float* vel, int substeps, uint32_t* ids,
                             int nthreads) {
-    if (check(p, n) || substeps < 1) return nullptr;
+    if (check(p, n) || substeps < 1 || p->completeNeighbours) return nullptr;  // the reference's sets only
     if (nthreads > 0) omp_set_num_threads(nthreads);
     Consts<float> c = make_consts<float>(*p);
     auto* rec = new RolloutRecord();

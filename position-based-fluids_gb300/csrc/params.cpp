@@ -88,6 +88,7 @@ extern "C" int pbf_load_parameters(const char* text, PbfParameters* p, int* unkn
         else if (key == "boxclamp") fields >> p->boxClamp;
         else if (key == "zerodistanceguard") fields >> p->zeroDistanceGuard;
         else if (key == "relaxedmath") fields >> p->relaxedMath;
+        else if (key == "completeneighbours") fields >> p->completeNeighbours;
         else if (key == "blockdims" || key == "blockorigin" || key == "jitter" || key == "seed") {
             // scene keys (pbf_load_scene)
         } else {

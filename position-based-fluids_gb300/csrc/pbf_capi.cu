@@ -193,6 +193,7 @@ DevConsts make_consts(const PbfParameters& p, int n) {
     c.clamp = p.boxClamp ? 1 : 0;
     c.guard = p.zeroDistanceGuard ? 1 : 0;
     c.relaxed = p.relaxedMath ? 1 : 0;
+    c.complete = p.completeNeighbours ? 1 : 0;
     c.dpScale = c.negGradSpiky / c.rho0;
     c.invPoly6q = 1.0f / c.poly6q;
     c.circles = (int)p.friendsCircles;
@@ -316,7 +317,7 @@ int check_batch_compatible(pbf_ctx* ctx, const std::vector<PbfParameters>& sp) {
                           a.surfaceTenstionDist == b.surfaceTenstionDist && a.friendsCircles == b.friendsCircles &&
                           a.particlesPerCircle == b.particlesPerCircle && a.gridBufSize == b.gridBufSize &&
                           a.boxClamp == b.boxClamp && a.zeroDistanceGuard == b.zeroDistanceGuard &&
-                          a.relaxedMath == b.relaxedMath;
+                          a.relaxedMath == b.relaxedMath && a.completeNeighbours == b.completeNeighbours;
         if (!same)
             return fail(ctx, PBF_ERR_INVALID,
                         "scene " + std::to_string(s) + " differs from scene 0 in a parameter scenes must share "
@@ -1430,6 +1431,8 @@ int pbf_rollout_forward(pbf_ctx* ctx, int substeps, int checkpoint_every) {
     if (is_batch(ctx)) return fail(ctx, PBF_ERR_UNSUPPORTED, "rollouts run on single-scene contexts");
     if (ctx->paused) return fail(ctx, PBF_ERR_STATE, "rollouts need an unpaused simulation");
     if (ctx->nquads > 0) return fail(ctx, PBF_ERR_UNSUPPORTED, "rollouts do not differentiate force planes");
+    if (ctx->params.completeNeighbours)
+        return fail(ctx, PBF_ERR_UNSUPPORTED, "rollouts follow the reference's neighbour sets (completeNeighbours 0)");
     if (substeps < 1 || checkpoint_every < 1) return fail(ctx, PBF_ERR_INVALID, "substeps and checkpoint_every must be >= 1");
     if (ctx->params.simIterations < 1 || ctx->params.simIterations > 64)
         return fail(ctx, PBF_ERR_INVALID, "rollouts need 1..64 solver iterations");

@@ -31,6 +31,7 @@ struct DevConsts {
     float lo[3], hi[3];
     int clamp, guard;
     int relaxed;                 // relaxedMath: the neighbour passes' relaxed variants
+    int complete;                // completeNeighbours: all circles in every pass, self in the density
     int nquads, maskW, maskH;    // force planes (pbf_set_force_quads) and their mask
     const QuadDev* quads;
     const uint32_t* mask;        // NULL: the empty mask

@@ -172,8 +172,8 @@ struct FriendCircles {
             total += (int)byte_of(cnt, k);
             mt |= (uint64_t)byte_of(cnt, k) << (7 * k);
         }
-        mt |= (uint64_t)circles_kept(cnt, C, total, 0.6f) << 56;
-        mt |= (uint64_t)circles_kept(cnt, C, total, 0.5f) << 60;
+        mt |= (uint64_t)(c.complete ? C : circles_kept(cnt, C, total, 0.6f)) << 56;
+        mt |= (uint64_t)(c.complete ? C : circles_kept(cnt, C, total, 0.5f)) << 60;
         meta[i] = make_uint2((uint32_t)mt, (uint32_t)(mt >> 32));
     }
 };
@@ -487,8 +487,8 @@ build_friends_warp_kernel(DevConsts c, Batch b, const float4* __restrict__ pred,
         total += (int)byte_of(cnt, k);
         mt |= (uint64_t)byte_of(cnt, k) << (7 * k);
     }
-    mt |= (uint64_t)circles_kept(cnt, C, total, 0.6f) << 56;
-    mt |= (uint64_t)circles_kept(cnt, C, total, 0.5f) << 60;
+    mt |= (uint64_t)(c.complete ? C : circles_kept(cnt, C, total, 0.6f)) << 56;
+    mt |= (uint64_t)(c.complete ? C : circles_kept(cnt, C, total, 0.5f)) << 60;
     meta[i] = make_uint2((uint32_t)mt, (uint32_t)(mt >> 32));
 }
 
@@ -560,7 +560,8 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
     if (i < 0 || i >= n) return;
     const float4 pi = pred[i];
     const uint64_t mt = load_meta(meta, i);
-    float ds = 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
+    // complete neighbour sets count the particle itself first: d = h^2 - 0
+    float ds = c.complete ? c.h2 * c.h2 * c.h2 : 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
     constexpr int U = 4;
     gather_friends<U>(list, n, i, FriendRows(mt, kept_density(mt), c.perCircle),
                       [&](uint32_t j) { return __ldg(pred + j); }, [&](const float4 pj) {

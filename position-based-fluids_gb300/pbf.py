@@ -47,7 +47,7 @@ class PbfParameters(ctypes.Structure):
         ("setupSpacing", c_float), ("segmentSize", c_uint), ("sortIterations", c_uint),
         ("particleRenderSize", c_float), ("h_2", c_float), ("EnableCachedBuffers", c_bool),
         ("gravityVectorEnable", c_int), ("gravityX", c_float), ("gravityY", c_float), ("gravityZ", c_float),
-        ("boxClamp", c_int), ("zeroDistanceGuard", c_int), ("relaxedMath", c_int),
+        ("boxClamp", c_int), ("zeroDistanceGuard", c_int), ("relaxedMath", c_int), ("completeNeighbours", c_int),
     ]
 
     def copy(self) -> "PbfParameters":

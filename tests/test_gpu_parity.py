@@ -302,3 +302,26 @@ def test_rollout_1m_100_frames_bit_exact(pbf_mod, oracle_mod, cuda_device):
     rho = gpr[:, 3].astype(np.float64) / params.restDensity - 1.0
     print(f"1M after 200 substeps: density error mean {np.abs(rho).mean():.4f}, "
           f"kinetic {0.5 * np.sum(gv[:, :3].astype(np.float64) ** 2):.1f}")
+
+
+@pytest.mark.parametrize("algorithm", [0, 2], ids=["scan", "brick"])
+def test_complete_neighbours_bit_exact(pbf_mod, oracle_mod, cuda_device, algorithm):
+    """completeNeighbours 1 (every friend circle in every pass, self in the
+    density): GPU and oracle agree bit for bit, and the rule does change the
+    result against the reference's truncated sets."""
+    params, pos, vel = scene(pbf_mod, (24, 24, 24))
+    params.completeNeighbours = 1
+    gp, gv, gpr, _, _ = run_gpu(pbf_mod, params, pos, vel, 4, cuda_device, algorithm=algorithm)
+    op, ov, opr = oracle_mod.step(params, pos, vel, 4)
+    assert_same("pos", gp, op)
+    assert_same("vel", gv, ov)
+    assert_same("pred", gpr, opr)
+    params.completeNeighbours = 0
+    rp, _, _ = oracle_mod.step(params, pos, vel, 4)
+    assert not np.array_equal(rp, op)
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        p2 = params.copy()
+        p2.completeNeighbours = 1
+        sim.set_params(p2)
+        with pytest.raises(pbf_mod.PbfError):
+            sim.rollout_forward(2, 1)  # rollouts follow the reference's sets

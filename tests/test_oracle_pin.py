@@ -210,3 +210,23 @@ def test_render_restatement_sanity(pbf_mod, oracle_mod):
     for mode in (1, 2):
         s, _, o = oracle_mod.render(cam, mode, params, pos)
         assert np.array_equal(s, o) and np.all((o >= 0.0) & (o <= 2.0))
+
+
+def test_complete_neighbours_density(pbf_mod, oracle_mod):
+    """One solver iteration, so that the density of both rules is taken at the
+    same predicted positions: every particle's complete density (every circle
+    plus its own W(0)) is at least its density over the reference's truncated
+    sets, and larger by at least the self term."""
+    params, pos, vel = pbf_mod.make_scene("dam_break_32k")
+    params.simIterations = 1
+    dens = {}
+    for complete in (0, 1):
+        p = params.copy()
+        p.completeNeighbours = complete
+        _, _, pr = oracle_mod.step(p, pos, vel, 1)
+        dens[complete] = pr[:, 3].astype(np.float64)
+    poly6, _, _ = oracle_mod.constants(params)
+    self_term = poly6 * float(np.float32(params.h_2)) ** 3
+    assert np.all(dens[1] - dens[0] >= 0.999 * self_term)
+    print(f"mean density / rest: reference sets {dens[0].mean() / params.restDensity:.3f}, "
+          f"complete {dens[1].mean() / params.restDensity:.3f}")
