@@ -176,6 +176,11 @@ def cpu_baseline(params, pos, vel, seconds: float) -> dict:
             "sample": f"{done} substep(s) of the {n}-particle scene from its initial state, {el:.1f} s"}
 
 
+def workload_name(scene: str, n: int, iters: int, sub: int) -> str:
+    return (f"{scene}: {n} particles (128x64x128 block, spacing 0.05, seeded jitter) in a 12.8x6.4x6.4 box; "
+            f"{iters} iterations x {sub} substeps per step (frame)")
+
+
 def reference_arm(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -201,8 +206,9 @@ def reference_arm(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
         "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": 1000.0 * el / done,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{args.scene}: {n} particles, {iters} iterations; one step = one substep",
-                   "threads": threads},
+        "config": {"workload": workload_name(args.scene, n, iters, int(params.subSteps)),
+                   "reference_step": "one substep per timed step (a bounded sample of the frame)",
+                   "particles": n, "iterations": iters, "threads": threads},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{done} substep(s) from the initial state (time budget {budget:.0f} s)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -374,8 +380,7 @@ def gpu_arm(args) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{args.scene}: {n} particles (128x64x128 block, spacing 0.05, seeded jitter) "
-                               f"in a 12.8x6.4x6.4 box; {iters} iterations x {sub} substeps per step (frame)",
+        "config": {"workload": workload_name(args.scene, n, iters, sub),
                    "particles": n, "iterations": iters, "substeps_per_step": sub,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "working set larger than L2 (no flush)", "mode": MODES[args.math],
