@@ -203,7 +203,7 @@ def reference_arm(args) -> None:
     el = time.perf_counter() - t0
     value = n * iters * done / el
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": 1000.0 * el / done,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload_name(args.scene, n, iters, int(params.subSteps)),
