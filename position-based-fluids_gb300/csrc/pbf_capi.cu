@@ -446,7 +446,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     uint32_t* list = tape ? tape->list : ctx->list;
     uint2* meta = tape ? tape->meta : ctx->meta;
     float4* omega = tape ? tape->omega : ctx->omega;
-    if (tape) cudaMemcpyAsync(tape->perm, ctx->perm[ctx->keysIdx], 4 * (size_t)c.n, cudaMemcpyDeviceToDevice, s);
+    if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->perm, ctx->perm[ctx->keysIdx], 4 * (size_t)c.n, cudaMemcpyDeviceToDevice, s));
     mark("updateCells");
     pbf::launch_update_cells(c.n, keys, ctx->cells, s);
     mark("buildFriendsList");
@@ -472,11 +472,11 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
         pack_density_kernel<<<(c.n + 255) / 256, 256, 0, s>>>(c.n, ctx->pred[a], ctx->density);
         ++launched;
     }
-    if (tape) cudaMemcpyAsync(tape->pI, ctx->pred[a], v4, cudaMemcpyDeviceToDevice, s);
+    if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->pI, ctx->pred[a], v4, cudaMemcpyDeviceToDevice, s));
     mark("updateVelocities");
     pbf::launch_update_velocities(c, ctx->pred[a], ctx->pos[sortedPos], ctx->pos[sortedPos ^ 1], ctx->vel[V],
                                   paused ? nullptr : ctx->idsTmp, ctx->ids, s);
-    if (tape) cudaMemcpyAsync(tape->v2, ctx->vel[V], v4, cudaMemcpyDeviceToDevice, s);
+    if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->v2, ctx->vel[V], v4, cudaMemcpyDeviceToDevice, s));
     mark("applyViscosity");
     pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, ls.viscosity, ls.balance, s);
     mark("applyVorticity");
@@ -1175,18 +1175,17 @@ int pbf_sort_state(pbf_ctx* ctx, const float* pred, uint32_t* keys, uint32_t* pe
         return fail(ctx, PBF_ERR_CUDA, std::string("pbf_sort_state: ") + cudaGetErrorString(e));
     }
     cudaStream_t s = ctx->stream;
-    cudaMemcpyAsync(dPred, pred, 16 * (size_t)n, cudaMemcpyHostToDevice, s);
-    cudaMemsetAsync(dCells, 0xFF, 8 * (size_t)grid, s);
+    auto keep = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };  // the first error of the sequence
+    keep(cudaMemcpyAsync(dPred, pred, 16 * (size_t)n, cudaMemcpyHostToDevice, s));
+    keep(cudaMemsetAsync(dCells, 0xFF, 8 * (size_t)grid, s));
     pbf::launch_compute_keys(ctx->consts, batch_of(ctx), dPred, k[0], pm[0], s);
     const int r = pbf::launch_radix_sort(ctx->plan, k, pm, dHist, nullptr, nullptr, nullptr, nullptr, s);
     pbf::launch_update_cells(n, k[r], dCells, s);
     const uint32_t nKeys = ((uint32_t)n + 2047u) / 2048u * 2048u;
-    if (keys) {
-        cudaMemcpyAsync(keys, k[r], 4 * (size_t)n, cudaMemcpyDeviceToHost, s);
-    }
-    if (perm) cudaMemcpyAsync(perm, pm[r], 4 * (size_t)n, cudaMemcpyDeviceToHost, s);
-    if (cells) cudaMemcpyAsync(cells, dCells, 8 * (size_t)grid, cudaMemcpyDeviceToHost, s);
-    e = cudaStreamSynchronize(s);
+    if (keys) keep(cudaMemcpyAsync(keys, k[r], 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    if (perm) keep(cudaMemcpyAsync(perm, pm[r], 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    if (cells) keep(cudaMemcpyAsync(cells, dCells, 8 * (size_t)grid, cudaMemcpyDeviceToHost, s));
+    keep(cudaStreamSynchronize(s));
     if (e == cudaSuccess) e = cudaGetLastError();
     cleanup();
     if (e != cudaSuccess) return fail(ctx, PBF_ERR_CUDA, std::string("pbf_sort_state: ") + cudaGetErrorString(e));
@@ -1465,8 +1464,8 @@ int pbf_rollout_backward(pbf_ctx* ctx, const float* dL_dx, float* dL_dv0, float*
     pbf::AdjointBuffers ab = ctx->adj;  // adjoint_substep swaps its pointers
     PBF_CUDA(ctx, cudaMemcpyAsync(ctx->adjById, dL_dx, v4, cudaMemcpyHostToDevice, s));
     pbf::scatter_by_id(n, ctx->ckptEnd.ids, ctx->adjById, ab.xb, s);
-    cudaMemsetAsync(ab.vb, 0, v4, s);
-    cudaMemsetAsync(ab.scalars, 0, 16, s);
+    PBF_CUDA(ctx, cudaMemsetAsync(ab.vb, 0, v4, s));
+    PBF_CUDA(ctx, cudaMemsetAsync(ab.scalars, 0, 16, s));
     ctx->launches += 1;
     const int segments = (int)ctx->ckpt.size();
     for (int sgm = segments - 1; sgm >= 0 && rc == PBF_OK; --sgm) {
