@@ -9,9 +9,10 @@ step is one 1/60 s frame = 2 substeps of Simulation::Step.
   value  : particle-iterations/s = N * iterations * substeps / time, with the
            state resident in HBM; CUDA events on the library's stream around
            K frames (after W warm-up frames), max over ranks.
-  e2e    : the same metric through the C-ABI with host buffers: every frame
-           copies positions + velocities in from pinned host memory, steps,
-           and copies them back out (wall clock).
+  e2e    : the same metric through the C-ABI with host buffers, over the same
+           frames (replayed from the state the timed frames started from):
+           every frame copies positions + velocities in from pinned host
+           memory, steps, and copies them back out (wall clock).
   roofline: the dominant kernel's algorithmic bytes per launch over its
            average launch time (CUDA events between stages on the library's
            stream, in a separate pass of the same frames), against the
@@ -259,6 +260,10 @@ def gpu_arm(args) -> None:
         sim.step_async(sub)
     sim.synchronize()
     blocks = sim.autotune(trial_substeps=2) if not args.no_autotune else sim.launch_shape()
+    # the state the timed frames start from, for the end-to-end replay below
+    h0pos = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+    h0vel = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+    sim.read_state_into(h0pos.data_ptr(), h0vel.data_ptr())
 
     # ---- timed region: K frames, state resident in HBM ----
     barrier()
@@ -278,24 +283,37 @@ def gpu_arm(args) -> None:
     ms *= 1000.0
 
     # ---- end to end through the C-ABI with pinned host buffers ----
+    # The same frames again: the state the timed frames started from is
+    # uploaded and stepped frame by frame, so both numbers time the same work.
+    end_pos = np.empty((n, 4), np.float32)
+    end_vel = np.empty((n, 4), np.float32)
+    sim.read_state_into(end_pos.ctypes.data, end_vel.ctypes.data)
     hpos = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
     hvel = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
-    sim.read_state_into(hpos.data_ptr(), hvel.data_ptr())
-    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    hpos.copy_(torch.from_numpy(end_pos))
+    hvel.copy_(torch.from_numpy(end_vel))
+    e2e_steps = max(1, min(args.steps, args.e2e_steps or args.steps))
     def e2e_frame():  # upload, step, download through the C-ABI; one wait per frame
         sim.write_state_async(hpos.data_ptr(), hvel.data_ptr())
         sim.step_async(sub)
         sim.read_state_async(hpos.data_ptr(), hvel.data_ptr())
         sim.synchronize()
 
-    for _ in range(3):
+    for _ in range(3):  # warm-up frames beyond the timed ones
         e2e_frame()
+    hpos.copy_(h0pos)
+    hvel.copy_(h0vel)
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_frame()
     e2e_s = time.perf_counter() - t0
     e2e_value, _ = replica_rate(n * iters * sub * e2e_steps, e2e_s, dist, "cuda")
+    # a full replay must end on the timed frames' final state, bit for bit
+    e2e_replay_identical = None
+    if e2e_steps == args.steps:
+        e2e_replay_identical = bool(np.array_equal(hpos.numpy().view(np.uint32), end_pos.view(np.uint32)) and
+                                    np.array_equal(hvel.numpy().view(np.uint32), end_vel.view(np.uint32)))
 
     # ---- density error of the state after the timed frames ----
     _, _, dpred = sim.read_state()
@@ -387,7 +405,8 @@ def gpu_arm(args) -> None:
                    "cuda_graph": True,
                    "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm", "balance"], blocks))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
-                "steps": e2e_steps},
+                "steps": e2e_steps, "frames": "the timed frames replayed from their start state",
+                "replay_bit_identical": e2e_replay_identical},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
@@ -682,7 +701,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--scene", default=SCENE)
-    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="end-to-end frames (0: as many as --steps)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--cpu-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

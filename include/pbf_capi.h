@@ -343,7 +343,10 @@ int pbf_rollout_forward(pbf_ctx* ctx, int substeps, int checkpoint_every);
    Outputs (any may be NULL): dL_dv0 (4 per particle, by original index) for
    the initial velocities, dL_dvisc for viscosityFactor, dL_dg (3) for the
    gravity vector.  Memory: one segment of intermediate values.  The context's
-   state is left at the end of the rollout. */
+   state is left at the end of the rollout.  Returns PBF_ERR_STATE when the
+   buffers, cells, kernels, parameters, pause flag, force planes, force mask or
+   wave wall were set after the forward pass (its substeps could no longer be
+   recomputed); run pbf_rollout_forward again. */
 int pbf_rollout_backward(pbf_ctx* ctx, const float* dL_dx, float* dL_dv0, float* dL_dvisc, float* dL_dg);
 
 /* ------------------------------------------------------ headless render -- */
@@ -398,7 +401,8 @@ int pbf_set_launch_shape(pbf_ctx* ctx, const int* blocks);
 /* Time `trial_substeps` substeps from the current state for each candidate
    block size (64, 128, 256, 512), the three friends algorithms and both balance
    settings, keep the fastest per kernel (the balance setting by the sum of
-   the solver passes), restore the state, and report the choice through
+   the solver passes), restore the state (positions, velocities, particle ids
+   and the per-stage trackers as they were), and report the choice through
    blocks_out (PBF_LAUNCH_SHAPE_FIELDS ints, may be NULL). */
 int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out);
 

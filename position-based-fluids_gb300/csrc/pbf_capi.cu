@@ -54,6 +54,10 @@ struct pbf_ctx {
     size_t histWords = 0;
     uint32_t cellsWords = 0;  // gridBufSize the cell table was allocated for
     int listSlots = 0;
+    int cellsN = 0;           // particle count the friend rows were allocated for
+    // bumped by every call that changes what a substep computes (buffers,
+    // cells, parameters, pause, force planes, wave wall)
+    uint64_t epoch = 0;
 
     // batch: scene s owns particles [sceneOffsets[s], sceneOffsets[s+1])
     std::vector<PbfParameters> sceneParams;  // empty for a single scene
@@ -101,13 +105,14 @@ struct pbf_ctx {
     std::vector<Checkpoint> ckpt;
     Checkpoint ckptEnd;
     int rollSubsteps = 0, rollEvery = 0;
+    uint64_t rollEpoch = 0;                  // epoch the forward pass ran under
     // reverse pass: one segment of tape plus the adjoint buffers, kept
     // between calls while (rollEvery, simIterations, boxClamp) stay the same
     std::vector<void*> tapeMem;
     std::vector<pbf::AdjointTape> tapes;
     pbf::AdjointBuffers adj{};
     float4* adjById = nullptr;
-    int tapeEvery = 0, tapeIters = 0, tapeClamp = -1;
+    int tapeEvery = 0, tapeIters = 0, tapeClamp = -1, tapeN = 0, tapeSlots = 0;
 };
 
 namespace pbf {
@@ -335,6 +340,9 @@ struct StageClock {
         cudaEvent_t event;
     };
     std::vector<Mark> marks;
+    ~StageClock() {  // events of a substep that failed before finish()
+        for (auto& m : marks) cudaEventDestroy(m.event);
+    }
     // `iteration` >= 0 names the tracker name_iteration, as
     // OCLPerfMon::GetTrackerEvent(name, iterationIndex) does (src/OCLPerfMon.cpp:3-31).
     int stage(const char* name, int iteration = -1) {
@@ -559,15 +567,27 @@ void free_tape(pbf_ctx* ctx) {
     ctx->tapes.clear();
     ctx->adj = pbf::AdjointBuffers{};
     ctx->adjById = nullptr;
-    ctx->tapeEvery = ctx->tapeIters = 0;
+    ctx->tapeEvery = ctx->tapeIters = ctx->tapeN = ctx->tapeSlots = 0;
     ctx->tapeClamp = -1;
+}
+
+// Checkpoints and tape are sized for the particle count and the friend rows
+// they were taken with; a new count or new friend limits drop them.
+void free_rollout(pbf_ctx* ctx) {
+    for (auto& k : ctx->ckpt) { dev_free(k.pos); dev_free(k.vel); dev_free(k.ids); }
+    ctx->ckpt.clear();
+    dev_free(ctx->ckptEnd.pos); dev_free(ctx->ckptEnd.vel); dev_free(ctx->ckptEnd.ids);
+    ctx->rollSubsteps = ctx->rollEvery = 0;
+    free_tape(ctx);
 }
 
 // One segment of tape (rollEvery substeps) and the adjoint buffers.
 int ensure_tape(pbf_ctx* ctx) {
     const int n = ctx->n, iters = (int)ctx->params.simIterations, every = ctx->rollEvery;
     const int clamp = ctx->params.boxClamp != 0;
-    if (ctx->tapeEvery == every && ctx->tapeIters == iters && ctx->tapeClamp == clamp) return PBF_OK;
+    if (ctx->tapeEvery == every && ctx->tapeIters == iters && ctx->tapeClamp == clamp && ctx->tapeN == n &&
+        ctx->tapeSlots == ctx->listSlots)
+        return PBF_OK;
     free_tape(ctx);
     const size_t v4 = 16 * (size_t)n;
     bool ok = true;
@@ -602,6 +622,8 @@ int ensure_tape(pbf_ctx* ctx) {
     ctx->tapeEvery = every;
     ctx->tapeIters = iters;
     ctx->tapeClamp = clamp;
+    ctx->tapeN = n;
+    ctx->tapeSlots = ctx->listSlots;
     return PBF_OK;
 }
 }  // namespace
@@ -679,9 +701,7 @@ int pbf_destroy(pbf_ctx* ctx) {
     dev_free(ctx->quadsDev); dev_free(ctx->maskDev); dev_free(ctx->waveDev);
     if (ctx->timingAnchor) cudaEventDestroy(ctx->timingAnchor);
     free_render(ctx);
-    for (auto& k : ctx->ckpt) { dev_free(k.pos); dev_free(k.vel); dev_free(k.ids); }
-    dev_free(ctx->ckptEnd.pos); dev_free(ctx->ckptEnd.vel); dev_free(ctx->ckptEnd.ids);
-    free_tape(ctx);
+    free_rollout(ctx);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PBF_OK;
@@ -696,7 +716,9 @@ int pbf_init_buffers(pbf_ctx* ctx, const float* init_pos, const float* init_vel)
     PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     drop_graph(ctx);
     const int n = (int)p.particleCount;
+    if (n != ctx->n) free_rollout(ctx);
     ctx->n = n;
+    ++ctx->epoch;
     int rc;
     for (int k = 0; k < 2; ++k) {
         if ((rc = dev_alloc(ctx, &ctx->pos[k], n)) || (rc = dev_alloc(ctx, &ctx->pred[k], n)) ||
@@ -741,6 +763,7 @@ int pbf_init_buffers(pbf_ctx* ctx, const float* init_pos, const float* init_vel)
     else PBF_CUDA(ctx, cudaMemset(ctx->vel[0], 0, 16 * (size_t)n));
     PBF_CUDA(ctx, cudaMemset(ctx->vel[1], 0, 16 * (size_t)n));
     ctx->buffersReady = true;
+    ctx->cellsReady = ctx->cellsReady && ctx->cellsN == n;  // friend rows are sized per particle
     ctx->kernelsReady = false;
     return PBF_OK;
 }
@@ -762,6 +785,8 @@ int pbf_init_cells(pbf_ctx* ctx) {
     PBF_CUDA(ctx, cudaMemset(ctx->cells, 0xFF, 8 * tableWords));
     ctx->cellsWords = p.gridBufSize;
     ctx->listSlots = (int)(p.friendsCircles * p.particlesPerCircle);
+    ctx->cellsN = ctx->n;
+    ++ctx->epoch;
     if ((rc = dev_alloc(ctx, &ctx->list, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->meta, ctx->n)))
         return rc;
     PBF_CUDA(ctx, cudaMemset(ctx->meta, 0, 8 * (size_t)ctx->n));
@@ -786,6 +811,7 @@ int pbf_load_force_masks(pbf_ctx* ctx, const uint32_t* mask, int width, int heig
         ctx->maskW = width;
         ctx->maskH = height;
     }
+    ++ctx->epoch;
     drop_graph(ctx);
     apply_planes(ctx);
     return PBF_OK;
@@ -806,6 +832,7 @@ int pbf_set_force_quads(pbf_ctx* ctx, const PbfForceQuad* quads, int count) {
         PBF_CUDA(ctx, cudaMemcpy(ctx->quadsDev, q.data(), sizeof(pbf::QuadDev) * count, cudaMemcpyHostToDevice));
         ctx->nquads = count;
     }
+    ++ctx->epoch;
     drop_graph(ctx);
     apply_planes(ctx);
     return PBF_OK;
@@ -983,6 +1010,7 @@ int pbf_set_wave_position(pbf_ctx* ctx, float wavePos) {
         drop_graph(ctx);  // the kernels now read the wall offset
         apply_planes(ctx);
     }
+    ++ctx->epoch;
     // stream-ordered: steps enqueued before see the old wall, steps after the new one
     PBF_CUDA(ctx, cudaMemcpyAsync(ctx->waveDev, &wavePos, sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
     PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1003,12 +1031,14 @@ int pbf_init_kernels(pbf_ctx* ctx) {
     if (!ctx->buffersReady || !ctx->cellsReady) return fail(ctx, PBF_ERR_STATE, "InitBuffers and InitCells must run before InitKernels");
     int rc = validate(ctx, ctx->params);
     if (rc) return rc;
-    if ((int)ctx->params.particleCount != ctx->n) return fail(ctx, PBF_ERR_INVALID, "particleCount changed since InitBuffers");
+    if ((int)ctx->params.particleCount != ctx->n || ctx->cellsN != ctx->n)
+        return fail(ctx, PBF_ERR_INVALID, "particleCount changed since InitBuffers or InitCells");
     if (ctx->params.gridBufSize != ctx->cellsWords ||
         (int)(ctx->params.friendsCircles * ctx->params.particlesPerCircle) != ctx->listSlots)
         return fail(ctx, PBF_ERR_INVALID, "gridBufSize or friend limits changed since InitCells");
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
     drop_graph(ctx);
+    ++ctx->epoch;
     ctx->consts = pbf::make_consts(ctx->params, ctx->n);
     apply_planes(ctx);
     uint64_t keyRange = ctx->params.gridBufSize;
@@ -1041,6 +1071,7 @@ int pbf_set_params(pbf_ctx* ctx, const PbfParameters* params) {
                             (int)(params->friendsCircles * params->particlesPerCircle) != ctx->listSlots))
         return fail(ctx, PBF_ERR_INVALID, "pbf_set_params cannot change gridBufSize or friend limits; re-run InitCells");
     ctx->params = *params;
+    ++ctx->epoch;
     if (ctx->kernelsReady) {
         drop_graph(ctx);
         ctx->consts = pbf::make_consts(ctx->params, ctx->n);
@@ -1051,6 +1082,7 @@ int pbf_set_params(pbf_ctx* ctx, const PbfParameters* params) {
 
 int pbf_set_pause(pbf_ctx* ctx, int paused) {
     if (!ctx) return fail(nullptr, PBF_ERR_INVALID, "NULL context");
+    if ((paused ? 1 : 0) != ctx->paused) ++ctx->epoch;
     ctx->paused = paused ? 1 : 0;
     return PBF_OK;
 }
@@ -1337,27 +1369,46 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
     const size_t n = (size_t)ctx->n;
     float4 *savePos = nullptr, *saveVel = nullptr;
     float* saveDensity = nullptr;
-    uint32_t* saveKeys = nullptr;
-    auto release = [&] { cudaFree(savePos); cudaFree(saveVel); cudaFree(saveDensity); cudaFree(saveKeys); };
+    uint32_t *saveKeys = nullptr, *saveIds = nullptr;
+    auto release = [&] {
+        cudaFree(savePos); cudaFree(saveVel); cudaFree(saveDensity); cudaFree(saveKeys); cudaFree(saveIds);
+    };
     if (cudaMalloc((void**)&savePos, 16 * n) || cudaMalloc((void**)&saveVel, 16 * n) ||
-        cudaMalloc((void**)&saveDensity, 4 * n) || cudaMalloc((void**)&saveKeys, 4 * n)) {
+        cudaMalloc((void**)&saveDensity, 4 * n) || cudaMalloc((void**)&saveKeys, 4 * n) ||
+        cudaMalloc((void**)&saveIds, 4 * n)) {
         release();
+        cudaGetLastError();
         return fail(ctx, PBF_ERR_CUDA, "pbf_autotune: cannot allocate the state copy");
     }
     const int pos0 = ctx->curPos, vel0 = ctx->curVel, pred0 = ctx->curPred, keys0 = ctx->keysIdx;
     const bool stepped0 = ctx->stepped, timing0 = ctx->stageTiming;
     const uint64_t launches0 = ctx->launches;
     const pbf::LaunchShape shape0 = ctx->shape;
-    cudaMemcpyAsync(savePos, ctx->pos[pos0], 16 * n, cudaMemcpyDeviceToDevice, ctx->stream);
-    cudaMemcpyAsync(saveVel, ctx->vel[vel0], 16 * n, cudaMemcpyDeviceToDevice, ctx->stream);
-    cudaMemcpyAsync(saveDensity, ctx->density, 4 * n, cudaMemcpyDeviceToDevice, ctx->stream);
-    cudaMemcpyAsync(saveKeys, ctx->keys[keys0], 4 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+    const std::vector<PbfPerfTracker> trackers0 = ctx->trackers;  // trials do not count as steps
+    // the trials step the state (and permute the particle records and their
+    // ids); the copy taken here is put back after each of them
+    auto copy_state = [&](bool back) {
+        struct { void* live; void* saved; size_t bytes; } parts[5] = {
+            {ctx->pos[pos0], savePos, 16 * n}, {ctx->vel[vel0], saveVel, 16 * n},
+            {ctx->density, saveDensity, 4 * n}, {ctx->keys[keys0], saveKeys, 4 * n}, {ctx->ids, saveIds, 4 * n}};
+        cudaError_t err = cudaSuccess;
+        for (const auto& q : parts) {
+            const cudaError_t e1 = back ? cudaMemcpyAsync(q.live, q.saved, q.bytes, cudaMemcpyDeviceToDevice, ctx->stream)
+                                        : cudaMemcpyAsync(q.saved, q.live, q.bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+            if (err == cudaSuccess) err = e1;
+        }
+        return err;
+    };
+    if (cudaError_t e0 = copy_state(false)) {
+        cudaStreamSynchronize(ctx->stream);
+        release();
+        return fail(ctx, PBF_ERR_CUDA, std::string("pbf_autotune: state copy: ") + cudaGetErrorString(e0));
+    }
+    cudaError_t restoreErr = cudaSuccess;
     auto restore = [&] {
         ctx->curPos = pos0; ctx->curVel = vel0; ctx->curPred = pred0; ctx->keysIdx = keys0;
-        cudaMemcpyAsync(ctx->pos[pos0], savePos, 16 * n, cudaMemcpyDeviceToDevice, ctx->stream);
-        cudaMemcpyAsync(ctx->vel[vel0], saveVel, 16 * n, cudaMemcpyDeviceToDevice, ctx->stream);
-        cudaMemcpyAsync(ctx->density, saveDensity, 4 * n, cudaMemcpyDeviceToDevice, ctx->stream);
-        cudaMemcpyAsync(ctx->keys[keys0], saveKeys, 4 * n, cudaMemcpyDeviceToDevice, ctx->stream);
+        const cudaError_t e1 = copy_state(true);
+        if (restoreErr == cudaSuccess) restoreErr = e1;
     };
     const char* names[5] = {"buildFriendsList", "computeScaling", "computeDelta", "applyViscosity", "applyVorticity"};
     const int candidates[4] = {64, 128, 256, 512};
@@ -1397,7 +1448,9 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
     int choice[5] = {friendsBlock, solverBlock[balance][0], solverBlock[balance][1], solverBlock[balance][2],
                      solverBlock[balance][3]};
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = restoreErr;
     release();
+    ctx->trackers = trackers0;
     ctx->stageTiming = timing0;
     ctx->stageNames.clear();
     ctx->stageMs.clear();
@@ -1447,6 +1500,7 @@ int pbf_rollout_forward(pbf_ctx* ctx, int substeps, int checkpoint_every) {
     if ((rc = save_checkpoint(ctx, ctx->ckptEnd))) return rc;
     ctx->rollSubsteps = substeps;
     ctx->rollEvery = checkpoint_every;
+    ctx->rollEpoch = ctx->epoch;
     return pbf_synchronize(ctx);
 }
 
@@ -1455,6 +1509,10 @@ int pbf_rollout_backward(pbf_ctx* ctx, const float* dL_dx, float* dL_dv0, float*
     if (rc) return rc;
     if (!dL_dx) return fail(ctx, PBF_ERR_INVALID, "pbf_rollout_backward: dL_dx is NULL");
     if (ctx->ckpt.empty() || ctx->rollSubsteps < 1) return fail(ctx, PBF_ERR_STATE, "pbf_rollout_forward has not run");
+    // the recomputed segments must be the substeps the forward pass took
+    if (ctx->rollEpoch != ctx->epoch)
+        return fail(ctx, PBF_ERR_STATE,
+                    "the buffers, parameters, pause, force planes or wave wall changed since pbf_rollout_forward");
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
     if ((rc = ensure_tape(ctx))) return rc;
     drop_graph(ctx);

@@ -58,6 +58,7 @@ def test_autotune_keeps_results_and_state(pbf_mod, cuda_device):
         b.Step(2)
         for x, y in zip(a.read_state(), b.read_state()):
             assert _same(x, y)
+        assert np.array_equal(a.read_ids(), b.read_ids())  # the trials' permutations are undone too
         b.set_launch_shape([96, 160, 224, 288, 352, (blocks[5] + 1) % 3, 1 - blocks[6]])  # another algorithm
         b.Step(1)
         a.Step(1)

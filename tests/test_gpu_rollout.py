@@ -138,6 +138,17 @@ def test_rollout_argument_errors(pbf_mod, case, cuda_device):
             sim.rollout_backward(np.zeros((params.particleCount, 4), np.float32))  # no forward yet
         with pytest.raises(pbf_mod.PbfError):
             sim.rollout_forward(0, 1)
+        # the reverse pass recomputes the forward's substeps: parameters set
+        # in between (here 65 solver iterations, beyond the tape's 64) are refused
+        sim.rollout_forward(2, 1)
+        p2 = params.copy()
+        p2.simIterations = 65
+        sim.set_params(p2)
+        with pytest.raises(pbf_mod.PbfError, match="changed since pbf_rollout_forward"):
+            sim.rollout_backward(np.zeros((params.particleCount, 4), np.float32))
+        sim.set_params(params)
+        sim.rollout_forward(2, 1)
+        sim.rollout_backward(np.zeros((params.particleCount, 4), np.float32))
         sim.bPauseSim = True
         with pytest.raises(pbf_mod.PbfError):
             sim.rollout_forward(2, 1)  # a paused simulation has no rollout
