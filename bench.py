@@ -231,6 +231,17 @@ def replica_rate(units: float, seconds: float, dist=None, device: str = "cpu") -
     return float(u.item()) / float(t.item()), float(t.item())
 
 
+# The stage groups the per-stage times are also reported in: keys, sort,
+# permutation and cell table / friend lists and the density pass / the
+# position-correction pass / velocities, XSPH and vorticity.
+STAGE_GROUPS = {
+    "sort": ("predictPositions", "radixsort", "sortParticles", "updateCells", "resetPartList"),
+    "friends+lambda": ("buildFriendsList", "computeScaling"),
+    "delta_p": ("computeDelta", "packData"),
+    "xsph+vorticity": ("updateVelocities", "applyViscosity", "applyVorticity"),
+}
+
+
 def gpu_arm(args) -> None:
     import numpy as np
     import torch
@@ -414,7 +425,9 @@ def gpu_arm(args) -> None:
         "pipeline_roofline": {"bytes_per_particle_substep": 444.0 + 56.0 * iters, "achieved": pipeline_gbs,
                               "frac": pipeline_gbs / peak},
         **({"issue_roofline": issue} if issue else {}),
+        "particle_substeps_per_s": value / iters,
         "stage_ms_per_step": {k: round(v, 4) for k, v in sorted(stage_ms.items(), key=lambda kv: -kv[1])},
+        "stage_groups_ms_per_step": {g: round(sum(stage_ms.get(k, 0.0) for k in ks), 4) for g, ks in STAGE_GROUPS.items()},
         "neighbours": {"density_pass": nl, "other_passes": nd},
         "density_error": density_error,
         **({"other_mode": other_line} if other_line else {}),
