@@ -134,6 +134,8 @@ SUBSTEP_CASES = {
     "zero_iterations": (dict(dims=(16, 16, 16), simIterations=0), 2),
     "one_iteration_odd": (dict(dims=(19, 7, 23), simIterations=1), 2),
     "collisions_clamped": (dict(dims=(16, 16, 16), gridBufSize=128), 2),
+    "eight_circles_64": (dict(dims=(16, 16, 16), friendsCircles=8, particlesPerCircle=64), 2),
+    "seven_circles_saturated": (dict(dims=(16, 16, 16), friendsCircles=7, particlesPerCircle=3), 2),
     "two_particles": (dict(dims=(2, 1, 1)), 3),
     "one_particle": (dict(dims=(1, 1, 1)), 2),
 }
