@@ -15,7 +15,9 @@ Two libraries:
   unit is compiled.
 
 Both are compiled with ``-ffp-contract=off`` so that every floating-point
-operation is rounded on its own, on x86-64 and on aarch64 alike.
+operation is rounded on its own, on x86-64 and on aarch64 alike, and with
+OpenMP: the restatement runs particles in parallel, the reference's kernels
+run their work-items in parallel (``ref_driver.inc``).
 """
 from __future__ import annotations
 
@@ -105,7 +107,7 @@ def build_ref(force: bool = False) -> Path | None:
         return None
     deps = [REF_TU, HERE / "clshim.hpp", HERE / "ref_driver.inc", HERE / "noise_sin.hpp"]
     if force or _stale(REF_LIB, deps):
-        _run(["g++", *CXXFLAGS, "-fwrapv", "-w", str(REF_TU), "-o", str(REF_LIB)])
+        _run(["g++", *CXXFLAGS, "-fopenmp", "-fwrapv", "-w", str(REF_TU), "-o", str(REF_LIB)])
     return REF_LIB
 
 

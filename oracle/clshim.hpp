@@ -166,8 +166,9 @@ inline void write_imagef(image2d_t, int2, float4) {}
 inline int get_image_width(image2d_t img) { return img ? img->width : 2048; }
 
 // ---- work-item ids ----
+// one per host thread: the driver runs work-items on several threads
 struct WorkItem { uint gid, lid, grp, ngroups, lsize; };
-extern WorkItem wi;
+extern thread_local WorkItem wi;
 inline uint get_global_id(int) { return wi.gid; }
 inline uint get_local_id(int) { return wi.lid; }
 inline uint get_group_id(int) { return wi.grp; }

@@ -81,6 +81,10 @@ def ref() -> ctypes.CDLL:
         l.ref_sort_f32.restype = c_int
         l.ref_set_force_mask.argtypes = [c_void_p, c_int, c_int]
         l.ref_set_force_mask.restype = None
+        l.ref_set_threads.argtypes = [c_int]
+        l.ref_set_threads.restype = None
+        l.ref_max_threads.argtypes = []
+        l.ref_max_threads.restype = c_int
         _ref = l
     return _ref
 
@@ -198,8 +202,14 @@ def max_threads() -> int:
     return int(lib().oracle_max_threads())
 
 
-def ref_step(params, pos, vel, substeps=1):
-    """The reference's kernels through the shim.  Returns (pos, vel, pred, keys, perm, cells)."""
+def ref_max_threads() -> int:
+    return int(ref().ref_max_threads())
+
+
+def ref_step(params, pos, vel, substeps=1, threads=0):
+    """The reference's kernels through the shim, work-items on `threads` host
+    threads (0: all).  Returns (pos, vel, pred, keys, perm, cells)."""
+    ref().ref_set_threads(int(threads))
     n = int(params.particleCount)
     pos = np.array(pos, np.float32, copy=True).reshape(n, 4)
     vel = np.array(vel, np.float32, copy=True).reshape(n, 4)

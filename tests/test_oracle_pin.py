@@ -111,6 +111,22 @@ def test_oracle_matches_reference_live(seed, substeps, overrides, pbf_mod, oracl
         assert np.array_equal(mg.canonical(x).view(np.uint32), mg.canonical(y).view(np.uint32)), name
 
 
+@needs_ref
+def test_reference_kernels_same_bits_on_one_and_all_threads(pbf_mod, oracle_mod):
+    """The shim runs work-items on several threads (applyViscosity on per-thread
+    copies of the pre-pass velocities); the result must not depend on how many."""
+    params = pbf_mod.load_scenario("dam_break_32k")
+    dims = (14, 12, 10)
+    params.particleCount = dims[0] * dims[1] * dims[2]
+    pos = pbf_mod.scene_block(*dims, 0.05, (0.3, 0.2, 0.1), 0.01, 11)
+    vel = np.zeros_like(pos)
+    vel[:, :3] = np.random.default_rng(11).normal(0, 0.2, (len(pos), 3)).astype(np.float32)
+    one = oracle_mod.ref_step(params, pos, vel, 3, threads=1)
+    every = oracle_mod.ref_step(params, pos, vel, 3, threads=0)
+    for a, b in zip(one, every):
+        assert np.array_equal(np.ascontiguousarray(a).view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
+
+
 def test_fp64_oracle_close_to_fp32(pbf_mod, oracle_mod):
     """The FP64 oracle runs the same pipeline; one substep stays close."""
     params = pbf_mod.load_scenario("dam_break_32k")
