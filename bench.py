@@ -63,21 +63,17 @@ STAGE_BYTES = {
     "applyVorticity": lambda nl, nd: 68.0 + 4.0 * nd,
 }
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
-# density pass, from `ncu --set full` on this workload at an early frame where
-# the density pass used 22.3 friends per particle (profiles/
-# compute_scaling_dam_break_1m.md).  Its traffic is dominated by the
-# friend-list rows, so it is scaled to the timed state by the per-particle
-# algorithmic bytes (40 + 4 nl).
-# DRAM bytes (read + write) of one launch from an ncu capture of the
-# dam_break_1m scene after 50 frames, with the mean list length then; scaled
-# to the measured list length by the stage's algorithmic bytes.
-TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 307.58e6, "nl": 31.19},
-                   "computeDelta": {"bytes": 268.21e6, "nl": 26.99}}
-# Warp instructions of one exact-mode launch from the same capture (256-thread
-# blocks), with its mean list length; scaled by the list length measured.
-ISSUE_CAPTURE = {"computeScaling": {"inst": 163.26e6, "nl": 31.19},
-                 "computeDelta": {"inst": 167.33e6, "nl": 26.99}}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and warp
+# instructions (smsp__inst_executed.sum) of one exact-mode launch, from ncu
+# captures of the dam_break_1m scene in the first substep of frame 51 (256-thread
+# blocks, plain thread map), with the mean list lengths of that substep (density
+# pass nl, other passes nd).  Scaled to the measured list lengths: the traffic
+# by the stage's algorithmic bytes, the instructions in proportion to the list
+# length of the pass.
+TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 307.58e6, "nl": 38.88, "nd": 33.07},
+                   "computeDelta": {"bytes": 268.21e6, "nl": 38.88, "nd": 33.07}}
+ISSUE_CAPTURE = {"computeScaling": {"inst": 163.26e6, "nl": 38.88, "nd": 33.07},
+                 "computeDelta": {"inst": 167.33e6, "nl": 38.88, "nd": 33.07}}
 SM_COUNT = 152
 SCHEDULERS_PER_SM = 4
 
@@ -376,19 +372,19 @@ def gpu_arm(args) -> None:
     traffic = None
     if dominant in TRAFFIC_CAPTURE:
         cap = TRAFFIC_CAPTURE[dominant]
-        scale = STAGE_BYTES[dominant](nl, nd) / STAGE_BYTES[dominant](cap["nl"], cap["nl"])
+        scale = STAGE_BYTES[dominant](nl, nd) / STAGE_BYTES[dominant](cap["nl"], cap["nd"])
         traffic = cap["bytes"] * scale
     issue = None
     if dominant in ISSUE_CAPTURE and args.math == "exact":
         cap = ISSUE_CAPTURE[dominant]
-        inst = cap["inst"] * ((nl if dominant == "computeScaling" else nd) / cap["nl"])
+        inst = cap["inst"] * (nl / cap["nl"] if dominant == "computeScaling" else nd / cap["nd"])
         clk = clocks.summary().get("sm_mhz") or 2070.0
         peak_issue = SM_COUNT * SCHEDULERS_PER_SM * clk * 1e6
         issue = {"kernel": dominant, "warp_instructions_per_launch": inst,
                  "achieved": inst / (launch_ms / 1000.0), "peak": peak_issue, "unit": "warp instructions/s",
                  "frac": inst / (launch_ms / 1000.0) / peak_issue,
-                 "source": "ncu smsp__inst_executed.sum of one launch after 50 frames (256-thread blocks, plain "
-                           "thread map), scaled by list length"}
+                 "source": "ncu smsp__inst_executed.sum of one launch in the first substep of frame 51 (256-thread "
+                           "blocks, plain thread map, list length 38.88 / 33.07), scaled by list length"}
     # ---- the other arithmetic mode, same scene state, its own block sizes ----
     other_line = None
     if not args.no_other_mode:
