@@ -15,8 +15,15 @@ def _same(a, b):
     return np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
-def test_batch_equals_scenes_run_alone(pbf_mod, cuda_device):
+@pytest.mark.parametrize("contract", [{}, {"relaxedMath": 1}, {"completeNeighbours": 1}],
+                         ids=["exact", "relaxed", "complete"])
+def test_batch_equals_scenes_run_alone(pbf_mod, cuda_device, contract):
+    """Under every arithmetic contract and neighbour rule, each scene of a
+    batch is bit-identical to the same scene run alone."""
     scenes, positions = pbf_mod.make_batch_scenes(first=12)
+    for p in scenes:
+        for k, v in contract.items():
+            setattr(p, k, v)
     pos = np.concatenate(positions)
     with pbf_mod.Simulation.create(scenes, pos, np.zeros_like(pos), device=cuda_device) as sim:
         offs = sim.scene_offsets()
