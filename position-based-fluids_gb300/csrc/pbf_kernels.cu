@@ -144,36 +144,59 @@ __device__ __forceinline__ int circles_kept(uint64_t cnt, int C, int total, floa
 // are dropped, :79-83).  The circle is read off precomputed r^2 thresholds
 // (DevConsts::circT): the same integer the sqrt / divide / cube / truncate
 // sequence gives, without computing it.
+//
+// Narrow (at most 5 circles of at most 63): the counters are 6-bit fields of
+// one word and a candidate is taken without a branch: its slot, the
+// predicate "inside and its circle not full", a predicated store and a
+// predicated increment.  Nearly every step of a warp has some lane that
+// accepts, so a branch would run the accept path for a few lanes anyway.
+// Either form writes the same entries in the same order.
+template <bool Narrow>
 struct FriendCircles {
     const DevConsts& c;
-    uint32_t* list;
+    uint32_t* row0;     // this particle's entry of list row 0; row r is row0 + r * n
+    uint32_t rowBytes;  // 4 n
     int n, i;
     float4 pi;
-    uint64_t cnt = 0;  // 8 circles x 8-bit counters
+    uint64_t cnt = 0;   // wide: 8 circles x 8-bit counters
+    uint32_t cnt6 = 0;  // narrow: 5 circles x 6-bit counters
     __device__ __forceinline__ FriendCircles(const DevConsts& cc, uint32_t* l, int i_, float4 p)
-        : c(cc), list(l), n(cc.n), i(i_), pi(p) {}
+        : c(cc), row0(l + i_), rowBytes(4u * (uint32_t)cc.n), n(cc.n), i(i_), pi(p) {}
+    __device__ __forceinline__ uint32_t count(int k) const {
+        return Narrow ? (cnt6 >> (6 * k)) & 63u : byte_of(cnt, k);
+    }
     __device__ __forceinline__ void consider(uint32_t j, const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-        if (r2 >= c.h2) return;
         // thresholds past C-1 are +inf, so only the first C-1 decide
         int circ = (r2 >= c.circT[0]) + (r2 >= c.circT[1]) + (r2 >= c.circT[2]) + (r2 >= c.circT[3]);
-        if (c.circles > 5) circ += (r2 >= c.circT[4]) + (r2 >= c.circT[5]) + (r2 >= c.circT[6]);
-        const uint32_t k = byte_of(cnt, circ);
-        if ((int)k >= c.perCircle) return;
-        list[(size_t)(circ * c.perCircle + (int)k) * n + i] = j;
-        cnt += 1ull << (8 * circ);
+        if (Narrow) {
+            const uint32_t sh = 6u * (uint32_t)circ;
+            const uint32_t k = (cnt6 >> sh) & 63u;
+            const bool take = !(r2 >= c.h2) && (int)k < c.perCircle;  // NaN distances are taken, as in the scan
+            const uint32_t row = (uint32_t)circ * (uint32_t)c.perCircle + k;
+            if (take) *reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(row0) + (size_t)row * rowBytes) = j;
+            cnt6 += take ? 1u << sh : 0u;
+        } else {
+            if (r2 >= c.h2) return;
+            if (c.circles > 5) circ += (r2 >= c.circT[4]) + (r2 >= c.circT[5]) + (r2 >= c.circT[6]);
+            const uint32_t k = byte_of(cnt, circ);
+            if ((int)k >= c.perCircle) return;
+            row0[(size_t)(circ * c.perCircle + (int)k) * n] = j;
+            cnt += 1ull << (8 * circ);
+        }
     }
     __device__ __forceinline__ void finish(uint2* meta) const {
         const int C = c.circles;
         int total = 0;
-        uint64_t mt = 0;
+        uint64_t mt = 0, bytes = 0;
         for (int k = 0; k < C; ++k) {
-            total += (int)byte_of(cnt, k);
-            mt |= (uint64_t)byte_of(cnt, k) << (7 * k);
+            total += (int)count(k);
+            mt |= (uint64_t)count(k) << (7 * k);
+            bytes |= (uint64_t)count(k) << (8 * k);
         }
-        mt |= (uint64_t)(c.complete ? C : circles_kept(cnt, C, total, 0.6f)) << 56;
-        mt |= (uint64_t)(c.complete ? C : circles_kept(cnt, C, total, 0.5f)) << 60;
+        mt |= (uint64_t)(c.complete ? C : circles_kept(bytes, C, total, 0.6f)) << 56;
+        mt |= (uint64_t)(c.complete ? C : circles_kept(bytes, C, total, 0.5f)) << 60;
         meta[i] = make_uint2((uint32_t)mt, (uint32_t)(mt >> 32));
     }
 };
@@ -183,10 +206,9 @@ struct FriendCircles {
 // cell in sorted order), self excluded, candidates read through L1 with U
 // loads in flight.  The 27 hashes are formed from the three spread
 // coordinates of each axis.
-template <int U>
+template <int U, typename FC>
 __device__ __forceinline__ void friends_scan_global(const DevConsts& c, uint32_t base, const float4* __restrict__ pred,
-                                                   const uint2* __restrict__ cells, int* __restrict__ err,
-                                                   FriendCircles& fc) {
+                                                   const uint2* __restrict__ cells, int* __restrict__ err, FC& fc) {
     const int i = fc.i, n = c.n;
     const float4 pi = fc.pi;
     const int cx = __float2int_rz(pi.x / c.h), cy = __float2int_rz(pi.y / c.h), cz = __float2int_rz(pi.z / c.h);
@@ -231,13 +253,13 @@ __device__ __forceinline__ void friends_scan_global(const DevConsts& c, uint32_t
 }
 
 // One thread per particle, candidates through L1.
-template <int U>
+template <int U, bool Narrow>
 __global__ void __launch_bounds__(kMaxBlock)
 build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const uint2* __restrict__ cells,
                      uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
-    FriendCircles fc(c, list, i, pred[i]);
+    FriendCircles<Narrow> fc(c, list, i, pred[i]);
     friends_scan_global<U>(c, key_base(b, i), pred, cells, err, fc);
     fc.finish(meta);
 }
@@ -263,7 +285,7 @@ __device__ __forceinline__ uint32_t compact_bits(uint32_t x) {
     return x;
 }
 
-template <int B>
+template <int B, bool Narrow>
 __global__ void __launch_bounds__(BrickShape<B>::threads)
 build_friends_brick_kernel(DevConsts c, const float4* __restrict__ pred, const uint2* __restrict__ cells,
                            uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
@@ -341,7 +363,7 @@ build_friends_brick_kernel(DevConsts c, const float4* __restrict__ pred, const u
     __syncthreads();
     for (uint32_t p = firstP + t; p <= lastP; p += T) {
         const int i = (int)p;
-        FriendCircles fc(c, list, i, pred[i]);
+        FriendCircles<Narrow> fc(c, list, i, pred[i]);
         const int cx = __float2int_rz(fc.pi.x / c.h), cy = __float2int_rz(fc.pi.y / c.h), cz = __float2int_rz(fc.pi.z / c.h);
         const int lx = cx - bx, ly = cy - by, lz = cz - bz;
         if (useSmem && (unsigned)lx < (unsigned)B && (unsigned)ly < (unsigned)B && (unsigned)lz < (unsigned)B) {
@@ -863,12 +885,15 @@ void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const
     const bool pow2 = (c.grid & (c.grid - 1)) == 0;
     const uint32_t keys = c.grid * (uint32_t)(b.scenes ? b.nscenes : 1);
     const uint2* cellPairs = reinterpret_cast<const uint2*>(cells);
+    // narrow counters: at most 5 circles of at most 63 friends
+    const bool narrow = c.circles <= 5 && c.perCircle <= 63;
     if (algorithm == 2 && pow2 && c.grid >= 64) {  // one block per 4x4x4-cell brick over all scenes
-        build_friends_brick_kernel<4><<<keys / 64u, BrickShape<4>::threads, 0, s>>>(c, pred, cellPairs, list, meta,
-                                                                                 errorWord);
+        auto kb = narrow ? build_friends_brick_kernel<4, true> : build_friends_brick_kernel<4, false>;
+        kb<<<keys / 64u, BrickShape<4>::threads, 0, s>>>(c, pred, cellPairs, list, meta, errorWord);
         return;
     }
-    auto k = algorithm == 1 ? build_friends_warp_kernel : build_friends_kernel<2>;
+    auto k = algorithm == 1 ? build_friends_warp_kernel
+                            : (narrow ? build_friends_kernel<2, true> : build_friends_kernel<2, false>);
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, reinterpret_cast<const uint2*>(cells), list, meta, errorWord);
 }
 
