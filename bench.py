@@ -97,15 +97,17 @@ class ClockSampler:
         self.device = device_index
         self.proc = None
         self.path = None
+        self.out = None
         self._summary = None
 
     def __enter__(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
+            self.out = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={CLOCK_FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                stdout=self.out, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         deadline = time.time() + 3.0  # the first sample before the timed region starts
@@ -126,6 +128,8 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+        if self.out is not None:
+            self.out.close()
 
     def summary(self) -> dict:
         if self._summary is None:
