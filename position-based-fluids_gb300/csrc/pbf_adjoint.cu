@@ -81,7 +81,7 @@ adj_vorticity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
     F3 eta = {0.0f, 0.0f, 0.0f};
     FriendRows f1(mt, kept_other(mt), c.perCircle);
     for (int t = 0; t < f1.total; ++t) {
-        const uint32_t j = list[(size_t)f1.row(t) * n + i];
+        const uint32_t j = checked_index(list[(size_t)f1.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const float4 pj = pI[j];
         const F3 r = pi - f3(pj);
         const float r2 = dot(r, r);
@@ -99,7 +99,7 @@ adj_vorticity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
     const F3 etab = (1.0f / l) * (Nb - dot(N, Nb) * N);
     FriendRows f2(mt, kept_other(mt), c.perCircle);
     for (int t = 0; t < f2.total; ++t) {
-        const uint32_t j = list[(size_t)f2.row(t) * n + i];
+        const uint32_t j = checked_index(list[(size_t)f2.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const float4 pj = pI[j];
         const F3 r = pi - f3(pj);
         const float r2 = dot(r, r);
@@ -132,7 +132,7 @@ adj_viscosity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
         add3(&v2b[i], v3b);
         FriendRows fr(mt, kept_other(mt), c.perCircle);
         for (int t = 0; t < fr.total; ++t) {
-            const uint32_t j = list[(size_t)fr.row(t) * n + i];
+            const uint32_t j = checked_index(list[(size_t)fr.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
             const float4 pj = pI[j];
             const F3 r = pi - f3(pj);
             const float r2 = dot(r, r);
@@ -190,7 +190,7 @@ adj_delta_kernel(DevConsts c, const float4* __restrict__ q, const uint8_t* __res
     const uint64_t mt = load_meta(meta, i);
     FriendRows fr(mt, kept_other(mt), c.perCircle);
     for (int t = 0; t < fr.total; ++t) {
-        const uint32_t j = list[(size_t)fr.row(t) * n + i];
+        const uint32_t j = checked_index(list[(size_t)fr.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const float4 qj = q[j];
         const F3 r = pi - f3(qj);
         const float r2 = dot(r, r);
@@ -226,7 +226,7 @@ adj_scaling_kernel(DevConsts c, const float4* __restrict__ q, const float* __res
     F3 S = {0.0f, 0.0f, 0.0f};
     FriendRows f1(mt, kept_density(mt), c.perCircle);
     for (int t = 0; t < f1.total; ++t) {
-        const uint32_t j = list[(size_t)f1.row(t) * n + i];
+        const uint32_t j = checked_index(list[(size_t)f1.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const F3 r = pi - f3(q[j]);
         const float r2 = dot(r, r);
         if (!in_support(c, r2)) continue;
@@ -242,7 +242,7 @@ adj_scaling_kernel(DevConsts c, const float4* __restrict__ q, const float* __res
     const float Db = lbar * Cc / (den * den) / c.rho0sq;
     FriendRows f2(mt, kept_density(mt), c.perCircle);
     for (int t = 0; t < f2.total; ++t) {
-        const uint32_t j = list[(size_t)f2.row(t) * n + i];
+        const uint32_t j = checked_index(list[(size_t)f2.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const F3 r = pi - f3(q[j]);
         const float r2 = dot(r, r);
         if (!in_support(c, r2)) continue;

@@ -281,6 +281,7 @@ void apply_planes(pbf_ctx* ctx) {
     ctx->consts.maskW = ctx->maskW;
     ctx->consts.maskH = ctx->maskH;
     ctx->consts.wave = ctx->waveDev;
+    ctx->consts.err = ctx->errWord;
 }
 
 void drop_graph(pbf_ctx* ctx) {
@@ -442,7 +443,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
         launched += pbf::radix_sort_launches(ctx->plan);
         mark("sortParticles");
         pbf::launch_gather_sorted(c.n, ctx->perm[ctx->keysIdx], ctx->pos[P], ctx->pred[0], ctx->ids, ctx->pos[P ^ 1],
-                                  ctx->pred[1], ctx->idsTmp, s);
+                                  ctx->pred[1], ctx->idsTmp, ctx->errWord, s);
         ++launched;
         sortedPos = P ^ 1;
         sortedPred = 1;
@@ -456,12 +457,13 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     float4* omega = tape ? tape->omega : ctx->omega;
     if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->perm, ctx->perm[ctx->keysIdx], 4 * (size_t)c.n, cudaMemcpyDeviceToDevice, s));
     mark("updateCells");
-    pbf::launch_update_cells(c.n, keys, ctx->cells, s);
+    const uint32_t tableKeys = ctx->cellsWords * (uint32_t)(is_batch(ctx) ? ctx->sceneParams.size() : 1);
+    pbf::launch_update_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s);
     mark("buildFriendsList");
     pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, meta, ctx->errWord, ls.friends,
                               ls.friendsAlgorithm, s);
     mark("resetPartList");
-    pbf::launch_reset_cells(c.n, keys, ctx->cells, s);
+    pbf::launch_reset_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s);
     launched += 3;
     int a = sortedPred;
     const unsigned iters = ctx->params.simIterations;
@@ -535,7 +537,12 @@ int read_error_word(pbf_ctx* ctx) {
     PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (word) {
         PBF_CUDA(ctx, cudaMemsetAsync(ctx->errWord, 0, sizeof(int), ctx->stream));
-        return fail(ctx, PBF_ERR_DEVICE_FLAG, "a kernel reported an inconsistent cell table (error word " + std::to_string(word) + ")");
+        std::string what;
+        if (word & pbf::kErrCellTable) what += ", an inconsistent cell table";
+        if (word & pbf::kErrFriendIndex) what += ", a friend-list entry out of range";
+        if (word & pbf::kErrSortIndex) what += ", a permutation entry out of range";
+        if (word & pbf::kErrCellKey) what += ", a key beyond the cell table";
+        return fail(ctx, PBF_ERR_DEVICE_FLAG, "a kernel reported" + what.substr(1) + " (error word " + std::to_string(word) + ")");
     }
     return PBF_OK;
 }
@@ -1212,7 +1219,7 @@ int pbf_sort_state(pbf_ctx* ctx, const float* pred, uint32_t* keys, uint32_t* pe
     keep(cudaMemsetAsync(dCells, 0xFF, 8 * (size_t)grid, s));
     pbf::launch_compute_keys(ctx->consts, batch_of(ctx), dPred, k[0], pm[0], s);
     const int r = pbf::launch_radix_sort(ctx->plan, k, pm, dHist, nullptr, nullptr, nullptr, nullptr, s);
-    pbf::launch_update_cells(n, k[r], dCells, s);
+    pbf::launch_update_cells(n, k[r], dCells, grid, nullptr, s);
     const uint32_t nKeys = ((uint32_t)n + 2047u) / 2048u * 2048u;
     if (keys) keep(cudaMemcpyAsync(keys, k[r], 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
     if (perm) keep(cudaMemcpyAsync(perm, pm[r], 4 * (size_t)n, cudaMemcpyDeviceToHost, s));

@@ -23,6 +23,12 @@ struct QuadDev {
     int maskYOffset, maskHeight;
 };
 
+// Bits of the device error word (pbf_synchronize reports it).
+constexpr int kErrCellTable = 1;    // a cell range that runs backwards
+constexpr int kErrFriendIndex = 2;  // a friend-list entry >= N (bounds-checked builds)
+constexpr int kErrSortIndex = 4;    // a permutation entry >= N (bounds-checked builds)
+constexpr int kErrCellKey = 8;      // a key beyond the cell table (bounds-checked builds)
+
 struct DevConsts {
     float dt, h, h2, minR, hMinusMinR;
     float poly6, gradSpiky, negGradSpiky, poly6q;
@@ -36,6 +42,7 @@ struct DevConsts {
     const QuadDev* quads;
     const uint32_t* mask;        // NULL: the empty mask
     const float* wave;           // device scalar: the moving wall's offset from xMin (NULL: none)
+    int* err;                    // the context's error word (bounds-checked builds record bad indices there)
     float dpScale, invPoly6q;    // -gradSpiky / rho0 and 1 / poly6q (relaxed variants only)
     int circles, perCircle;
     uint32_t grid;
@@ -85,10 +92,12 @@ void launch_predict_keys(const DevConsts& c, Batch b, const float4* pos, float4*
                          uint32_t* keys, uint32_t* perm, int paused, cudaStream_t s);
 void launch_compute_keys(const DevConsts& c, Batch b, const float4* pred, uint32_t* keys, uint32_t* perm,
                          cudaStream_t s);
+// err (may be NULL): the error word that bounds-checked builds report bad
+// permutation entries or keys to; keyLimit: the number of cell-table entries.
 void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, const uint32_t* ids,
-                          float4* posOut, float4* predOut, uint32_t* idsOut, cudaStream_t s);
-void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
-void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s);
+                          float4* posOut, float4* predOut, uint32_t* idsOut, int* err, cudaStream_t s);
+void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
+void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
 // algorithm: LaunchShape::friendsAlgorithm
 void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
                           uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s);

@@ -90,10 +90,10 @@ __global__ void compute_keys_kernel(DevConsts c, Batch b, const float4* __restri
 __global__ void gather_sorted_kernel(int n, const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
                                      const float4* __restrict__ pred, const uint32_t* __restrict__ ids,
                                      float4* __restrict__ posOut, float4* __restrict__ predOut,
-                                     uint32_t* __restrict__ idsOut) {
+                                     uint32_t* __restrict__ idsOut, int* err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t j = perm[i];
+    const uint32_t j = checked_index(perm[i], (uint32_t)n, err, kErrSortIndex);
     posOut[i] = pos[j];
     predOut[i] = pred[j];
     idsOut[i] = ids[j];
@@ -101,12 +101,13 @@ __global__ void gather_sorted_kernel(int n, const uint32_t* __restrict__ perm, c
 
 // --------------------------------------------------------------- cells --
 // update_cells.cl:6-25 on a table that holds END_OF_CELL_LIST everywhere.
-__global__ void update_cells_kernel(int n, const uint32_t* __restrict__ keys, uint32_t* __restrict__ cells) {
+__global__ void update_cells_kernel(int n, const uint32_t* __restrict__ keys, uint32_t* __restrict__ cells,
+                                    uint32_t keyLimit, int* err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t k = keys[i];
+    const uint32_t k = checked_index(keys[i], keyLimit, err, kErrCellKey);
     if (i > 0) {
-        const uint32_t kp = keys[i - 1];
+        const uint32_t kp = checked_index(keys[i - 1], keyLimit, err, kErrCellKey);
         if (kp != k) {
             cells[2 * (size_t)k] = (uint32_t)i;
             cells[2 * (size_t)kp + 1] = (uint32_t)(i - 1);
@@ -118,10 +119,11 @@ __global__ void update_cells_kernel(int n, const uint32_t* __restrict__ keys, ui
 }
 
 // reset_grid.cl:6-14
-__global__ void reset_cells_kernel(int n, const uint32_t* __restrict__ keys, uint2* __restrict__ cells) {
+__global__ void reset_cells_kernel(int n, const uint32_t* __restrict__ keys, uint2* __restrict__ cells,
+                                   uint32_t keyLimit, int* err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    cells[keys[i]] = make_uint2(kEmpty, kEmpty);
+    cells[checked_index(keys[i], keyLimit, err, kErrCellKey)] = make_uint2(kEmpty, kEmpty);
 }
 
 // Number of leading circles a pass keeps: circles are visited in order and
@@ -239,7 +241,7 @@ __device__ __forceinline__ void friends_scan_global(const DevConsts& c, uint32_t
                 const uint2 range = cells[base + hm];
                 if (range.x == kEmpty) continue;
                 const uint32_t last = min(range.y, (uint32_t)(n - 1));
-                if (range.x > last) { atomicOr(err, 1); continue; }
+                if (range.x > last) { atomicOr(err, kErrCellTable); continue; }
                 if (hm == selfHash && range.x <= (uint32_t)i && (uint32_t)i <= last) {
                     // the particle's own table entry: skip itself (build_friends_list.cl:62)
                     if ((uint32_t)i > range.x) scan(range.x, (uint32_t)i - 1);
@@ -317,7 +319,7 @@ build_friends_brick_kernel(DevConsts c, const float4* __restrict__ pred, const u
         if (range.x != kEmpty) {
             const uint32_t last = min(range.y, (uint32_t)(n - 1));
             if (range.x <= last) count = last - range.x + 1u;
-            else atomicOr(err, 1);
+            else atomicOr(err, kErrCellTable);
         }
         hStart[h] = range.x;
         hCount[h] = count;
@@ -448,7 +450,7 @@ build_friends_warp_kernel(DevConsts c, Batch b, const float4* __restrict__ pred,
             const uint2 range = cells[rbase + (pow2 ? (m & gmask) : (m % c.grid))];
             if (range.x != kEmpty) {
                 const uint32_t last = min(range.y, (uint32_t)(n - 1));
-                if (range.x > last) atomicOr(err, 1);
+                if (range.x > last) atomicOr(err, kErrCellTable);
                 else { start = range.x; count = last - range.x + 1u; }
             }
         }
@@ -586,7 +588,7 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
     float ds = c.complete ? c.h2 * c.h2 * c.h2 : 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
     constexpr int U = 4;
     gather_friends<U>(list, n, i, FriendRows(mt, kept_density(mt), c.perCircle),
-                      [&](uint32_t j) { return __ldg(pred + j); }, [&](const float4 pj) {
+                      [&](uint32_t j) { return __ldg(pred + checked_index(j, (uint32_t)n, c.err, kErrFriendIndex)); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         if (R) {
             const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
@@ -643,7 +645,7 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const 
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     constexpr int U = 4;
     gather_friends<U>(list, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
-                      [&](uint32_t j) { return __ldg(pp + j); }, [&](const float4 pj) {
+                      [&](uint32_t j) { return __ldg(pp + checked_index(j, (uint32_t)n, c.err, kErrFriendIndex)); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         if (R) {
             const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
@@ -747,7 +749,7 @@ apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, co
     float vsx = 0.0f, vsy = 0.0f, vsz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
     constexpr int U = 4;
     gather_friends<U>(list, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
-                      [&](uint32_t j) { return PairRec{__ldg(pred + j), __ldg(velIn + j)}; }, [&](const PairRec& q) {
+                      [&](uint32_t j) { j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex); return PairRec{__ldg(pred + j), __ldg(velIn + j)}; }, [&](const PairRec& q) {
         const float4 pj = q.a;
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
@@ -802,7 +804,7 @@ apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
     constexpr int U = 4;
     gather_friends<U>(list, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
-                      [&](uint32_t j) { return PairRec{__ldg(pred + j), __ldg(omega + j)}; }, [&](const PairRec& q) {
+                      [&](uint32_t j) { j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex); return PairRec{__ldg(pred + j), __ldg(omega + j)}; }, [&](const PairRec& q) {
         const float4 pj = q.a;
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
@@ -868,16 +870,16 @@ void launch_compute_keys(const DevConsts& c, Batch b, const float4* pred, uint32
 }
 
 void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, const uint32_t* ids,
-                          float4* posOut, float4* predOut, uint32_t* idsOut, cudaStream_t s) {
-    gather_sorted_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, perm, pos, pred, ids, posOut, predOut, idsOut);
+                          float4* posOut, float4* predOut, uint32_t* idsOut, int* err, cudaStream_t s) {
+    gather_sorted_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, perm, pos, pred, ids, posOut, predOut, idsOut, err);
 }
 
-void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s) {
-    update_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, cells);
+void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s) {
+    update_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, cells, keyLimit, err);
 }
 
-void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, cudaStream_t s) {
-    reset_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, reinterpret_cast<uint2*>(cells));
+void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s) {
+    reset_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, reinterpret_cast<uint2*>(cells), keyLimit, err);
 }
 
 void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,

@@ -98,7 +98,7 @@ extern "C" int pbf_sort_state_noalloc(const PbfParameters* params, const float* 
     }
     if (e == cudaSuccess && d_cells) {
         e = cudaMemsetAsync(d_cells, 0xFF, 8 * (size_t)params->gridBufSize, s);
-        if (e == cudaSuccess) pbf::launch_update_cells((int)n, d_keys, d_cells, s);
+        if (e == cudaSuccess) pbf::launch_update_cells((int)n, d_keys, d_cells, params->gridBufSize, nullptr, s);
     }
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) return pbf::fail(nullptr, PBF_ERR_CUDA, std::string("pbf_sort_state_noalloc: ") + cudaGetErrorString(e));

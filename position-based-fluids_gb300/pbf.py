@@ -10,13 +10,17 @@ reference's ``LoadParameters`` (src/ParamUtils.cpp:24-100).  Errors raise
 from __future__ import annotations
 
 import ctypes
+import os
 from ctypes import POINTER, c_bool, c_char_p, c_float, c_int, c_size_t, c_uint, c_uint32, c_uint64, c_void_p
 from pathlib import Path
 
 import numpy as np
 
 PKG = Path(__file__).resolve().parent
-LIB_PATH = PKG / "libpbf_gb300.so"
+# PBF_CHECK_BOUNDS=1 selects the bounds-checked build of the same sources
+# (build.py --checked): indices read from device memory are checked before
+# use and reported through the error word.
+LIB_PATH = PKG / ("libpbf_gb300_checked.so" if os.environ.get("PBF_CHECK_BOUNDS") == "1" else "libpbf_gb300.so")
 
 PBF_OK = 0
 PBF_ERR_INVALID = -1
@@ -102,7 +106,8 @@ def library() -> ctypes.CDLL:
     if _lib is not None:
         return _lib
     if not LIB_PATH.exists():
-        raise FileNotFoundError(f"{LIB_PATH} is not built; run position-based-fluids_gb300/build.py")
+        raise FileNotFoundError(f"{LIB_PATH} is not built; run position-based-fluids_gb300/build.py"
+                                f"{' --checked' if 'checked' in LIB_PATH.name else ''}")
     lib = ctypes.CDLL(str(LIB_PATH))
     P = POINTER(PbfParameters)
     f32p, u32p = POINTER(c_float), POINTER(c_uint32)
