@@ -132,3 +132,42 @@ def test_non_finite_injection_matches_oracle(pbf_mod, oracle_mod, cuda_device):
         return a.view(np.uint32)
     assert np.array_equal(canon(gp), canon(op)) and np.array_equal(canon(gv), canon(ov))
     assert np.isnan(gp).any()
+
+
+class _DeviceArray:
+    """A device buffer described by the CUDA array interface (no copy)."""
+
+    def __init__(self, ptr: int, n: int):
+        self.__cuda_array_interface__ = {"shape": (n, 4), "typestr": "<f4", "data": (ptr, False),
+                                         "strides": None, "version": 2}
+
+
+def test_device_positions_stream_and_nvtx(pbf_mod, cuda_device):
+    """pbf_device_positions hands out the current position buffer (the headless
+    stand-in for the GL buffer the reference shares with its renderer); work
+    queued on the library's stream (pbf_get_stream) after an asynchronous step
+    sees the stepped positions without a wait; NVTX ranges around the stages
+    change nothing."""
+    torch = pytest.importorskip("torch")
+    params, pos, vel = pbf_mod.make_scene("dam_break_32k")
+    n = int(params.particleCount)
+    dev = torch.device("cuda", cuda_device)
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as a, \
+         pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as b:
+        a.step_async(3)
+        stream = torch.cuda.ExternalStream(a.stream(), device=dev)
+        with torch.cuda.stream(stream):
+            view = torch.as_tensor(_DeviceArray(a.device_positions(), n), device=dev)
+            copy = view.clone()  # ordered after the step on the library's stream
+        stream.synchronize()
+        p, _, _ = a.read_state()
+        assert _same(copy.cpu().numpy(), p)
+        # eager steps with and without NVTX ranges
+        a.use_graph(False)
+        b.use_graph(False)
+        b.Step(3)
+        b.enable_nvtx(True)
+        a.Step(2)
+        b.Step(2)
+        for x, y in zip(a.read_state(), b.read_state()):
+            assert _same(x, y)
