@@ -28,6 +28,20 @@ def test_every_declared_symbol_is_exported(built_lib, pbf_mod):
     assert set(pbf_mod.EXPORTED_SYMBOLS) <= declared
 
 
+def test_checked_build_exports_the_same_symbols():
+    """The bounds-checked build (build.py --checked) is a drop-in for the plain
+    library: built from the same sources with -DPBF_CHECK_BOUNDS into its own
+    object directory, it exports every declared symbol."""
+    from tests.conftest import load_pkg_build
+    pkg_build = load_pkg_build()
+    commands = pkg_build.compile_commands(checked=True)
+    assert all("-DPBF_CHECK_BOUNDS" in cmd for src, _, cmd in commands if src.suffix == ".cu")
+    assert all(obj.parent == pkg_build.OBJ_CHECKED for _, obj, _ in commands)
+    lib = ctypes.CDLL(str(pkg_build.build(checked=True)))
+    missing = [n for n in sorted(declared_functions()) if not hasattr(lib, n)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
 def test_create_without_device_or_with_bad_args(pbf_mod):
     from tests.conftest import has_cuda_device
     p = pbf_mod.load_scenario("dam_break_32k")
