@@ -31,3 +31,21 @@ def test_stage_byte_models_name_reported_stages():
     assert set(bench.STAGE_BYTES) <= stages
     for model in bench.STAGE_BYTES.values():
         assert model(30.0, 27.0) > 0
+
+
+def test_reference_arm_prints_the_contract_line():
+    """bench.py --impl reference (CPU only) prints one JSON line with the keys
+    the bench contract names, timed on a bounded sample."""
+    import json
+    import subprocess
+    run = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--scene", "dam_break_32k",
+                          "--steps", "2", "--cpu-budget", "1"], capture_output=True, text=True, timeout=600)
+    assert run.returncode == 0, run.stderr[-2000:]
+    lines = [l for l in run.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"] is True
+    for key in ("metric", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["cpu_baseline"]["kind"] in ("reference", "port") and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
