@@ -148,11 +148,10 @@ __device__ __forceinline__ int circles_kept(uint64_t cnt, int C, int total, floa
 // sequence gives, without computing it.
 //
 // Narrow (at most 5 circles of at most 63): the counters are 6-bit fields of
-// one word and a candidate is taken without a branch: its slot, the
-// predicate "inside and its circle not full", a predicated store and a
-// predicated increment.  Nearly every step of a warp has some lane that
-// accepts, so a branch would run the accept path for a few lanes anyway.
-// Either form writes the same entries in the same order.
+// one word, so a candidate's slot, the test "inside and its circle not full",
+// the store and the increment are a few 32-bit operations with no branch
+// (the wide form's 64-bit counter arithmetic is longer).  Either form writes
+// the same entries in the same order.
 template <bool Narrow>
 struct FriendCircles {
     const DevConsts& c;
