@@ -113,6 +113,17 @@ struct pbf_ctx {
     pbf::AdjointBuffers adj{};
     float4* adjById = nullptr;
     int tapeEvery = 0, tapeIters = 0, tapeClamp = -1, tapeN = 0, tapeSlots = 0;
+    // one CUDA graph per segment shape of the reverse pass: the segment's
+    // recompute and its adjoint substeps, for a segment length and the adjoint
+    // buffers' roles at its start (and their roles at its end)
+    struct SegmentGraph {
+        int len = 0;
+        int pos = 0, vel = 0;  // the position / velocity buffer roles it was captured with
+        pbf::AdjointBuffers pre{}, post{};
+        cudaGraphExec_t exec = nullptr;
+        size_t nodes = 0;
+    };
+    std::vector<SegmentGraph> segGraphs;
 };
 
 namespace pbf {
@@ -284,10 +295,23 @@ void apply_planes(pbf_ctx* ctx) {
     ctx->consts.err = ctx->errWord;
 }
 
-void drop_graph(pbf_ctx* ctx) {
+// The captured substep; the reverse pass's segment graphs are dropped with
+// it by drop_graph (they bake in the same constants, shapes and buffers).
+void drop_step_graph(pbf_ctx* ctx) {
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     ctx->graph = nullptr;
     ctx->graphPos = -1;
+}
+
+void drop_segment_graphs(pbf_ctx* ctx) {
+    for (auto& g : ctx->segGraphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    ctx->segGraphs.clear();
+}
+
+void drop_graph(pbf_ctx* ctx) {
+    drop_step_graph(ctx);
+    drop_segment_graphs(ctx);
 }
 
 int validate(pbf_ctx* ctx, const PbfParameters& p) {
@@ -569,6 +593,7 @@ int load_checkpoint(pbf_ctx* ctx, const pbf_ctx::Checkpoint& k) {
 }
 
 void free_tape(pbf_ctx* ctx) {
+    drop_segment_graphs(ctx);
     for (void* p : ctx->tapeMem) cudaFree(p);
     ctx->tapeMem.clear();
     ctx->tapes.clear();
@@ -631,6 +656,74 @@ int ensure_tape(pbf_ctx* ctx) {
     ctx->tapeClamp = clamp;
     ctx->tapeN = n;
     ctx->tapeSlots = ctx->listSlots;
+    return PBF_OK;
+}
+
+bool same_buffers(const pbf::AdjointBuffers& a, const pbf::AdjointBuffers& b) {
+    return a.xb == b.xb && a.vb == b.vb && a.xo == b.xo && a.vo == b.vo && a.pb == b.pb && a.pbt == b.pbt &&
+           a.omb == b.omb && a.v2b == b.v2b && a.xsb == b.xsb && a.lb == b.lb && a.scalars == b.scalars;
+}
+
+// One segment of the reverse pass (its `len` substeps recomputed into the
+// tape, then their adjoints in reverse) as a CUDA graph: captured once per
+// segment length and starting role of the adjoint buffers, replayed for every
+// segment of that shape.  Every checkpoint starts a segment with the same
+// buffer roles (an unpaused substep keeps them), so the same recompute fits
+// all of them.
+int run_segment_graph(pbf_ctx* ctx, int len, pbf::AdjointBuffers& ab) {
+    cudaStream_t s = ctx->stream;
+    const int pos0 = ctx->curPos, pred0 = ctx->curPred, keys0 = ctx->keysIdx;
+    pbf_ctx::SegmentGraph* hit = nullptr;
+    for (auto& g : ctx->segGraphs)
+        if (g.len == len && g.pos == pos0 && g.vel == ctx->curVel && same_buffers(g.pre, ab)) hit = &g;
+    if (!hit) {
+        pbf_ctx::SegmentGraph g;
+        g.len = len;
+        g.pos = pos0;
+        g.vel = ctx->curVel;
+        g.pre = ab;
+        const uint64_t launches0 = ctx->launches;
+        cudaGraph_t graph = nullptr;
+        PBF_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int rc = PBF_OK;
+        for (int k = 0; k < len && rc == PBF_OK; ++k) rc = enqueue_substep(ctx, nullptr, &ctx->tapes[k]);
+        for (int k = len - 1; k >= 0 && rc == PBF_OK; --k) pbf::adjoint_substep(ctx->consts, ctx->tapes[k], ab, s);
+        const cudaError_t e = cudaStreamEndCapture(s, &graph);
+        g.post = ab;
+        // the capture only recorded the work: roles and buffers as they were
+        ab = g.pre;
+        ctx->curPos = pos0; ctx->curPred = pred0; ctx->keysIdx = keys0;
+        ctx->launches = launches0;
+        if (rc != PBF_OK || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            if (rc != PBF_OK) return rc;
+            return fail(ctx, PBF_ERR_CUDA, std::string("reverse-pass graph capture: ") + cudaGetErrorString(e));
+        }
+        size_t count = 0;  // its kernel launches (the memsets and tape copies are not counted)
+        cudaGraphGetNodes(graph, nullptr, &count);
+        std::vector<cudaGraphNode_t> nodes(count);
+        if (count) cudaGraphGetNodes(graph, nodes.data(), &count);
+        for (cudaGraphNode_t node : nodes) {
+            cudaGraphNodeType type;
+            if (cudaGraphNodeGetType(node, &type) == cudaSuccess && type == cudaGraphNodeTypeKernel) ++g.nodes;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) return fail(ctx, PBF_ERR_CUDA, std::string("reverse-pass graph: ") + cudaGetErrorString(ei));
+        ctx->segGraphs.push_back(g);
+        hit = &ctx->segGraphs.back();
+    }
+    PBF_CUDA(ctx, cudaGraphLaunch(hit->exec, s));
+    ab = hit->post;
+    ctx->launches += hit->nodes;
+    // the replayed substeps leave the roles as the eager ones do: an unpaused
+    // substep keeps the position role and ends with the sorted keys and
+    // predictions in their second buffers
+    if (len > 0) {
+        ctx->keysIdx = ctx->plan.passes & 1;
+        ctx->curPred = 1;
+    }
     return PBF_OK;
 }
 }  // namespace
@@ -1522,7 +1615,7 @@ int pbf_rollout_backward(pbf_ctx* ctx, const float* dL_dx, float* dL_dv0, float*
                     "the buffers, parameters, pause, force planes or wave wall changed since pbf_rollout_forward");
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
     if ((rc = ensure_tape(ctx))) return rc;
-    drop_graph(ctx);
+    drop_step_graph(ctx);
     const int n = ctx->n, iters = (int)ctx->params.simIterations, every = ctx->rollEvery;
     const size_t v4 = 16 * (size_t)n;
     cudaStream_t s = ctx->stream;
@@ -1536,10 +1629,14 @@ int pbf_rollout_backward(pbf_ctx* ctx, const float* dL_dx, float* dL_dv0, float*
     for (int sgm = segments - 1; sgm >= 0 && rc == PBF_OK; --sgm) {
         if ((rc = load_checkpoint(ctx, ctx->ckpt[sgm]))) break;
         const int len = std::min(every, ctx->rollSubsteps - sgm * every);
-        for (int k = 0; k < len && rc == PBF_OK; ++k) rc = enqueue_substep(ctx, nullptr, &ctx->tapes[k]);
-        for (int k = len - 1; k >= 0 && rc == PBF_OK; --k) {
-            pbf::adjoint_substep(ctx->consts, ctx->tapes[k], ab, s);
-            ctx->launches += pbf::adjoint_launches(iters);
+        if (ctx->useGraph) {
+            rc = run_segment_graph(ctx, len, ab);
+        } else {
+            for (int k = 0; k < len && rc == PBF_OK; ++k) rc = enqueue_substep(ctx, nullptr, &ctx->tapes[k]);
+            for (int k = len - 1; k >= 0 && rc == PBF_OK; --k) {
+                pbf::adjoint_substep(ctx->consts, ctx->tapes[k], ab, s);
+                ctx->launches += pbf::adjoint_launches(iters);
+            }
         }
     }
     if (rc) return rc;

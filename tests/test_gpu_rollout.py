@@ -85,6 +85,30 @@ def test_adjoint_matches_fp64_adjoint(pbf_mod, case, cuda_device, every):
     assert _rel(own[0][:, :3], dv64[:, :3]) < GRAD_TOL
 
 
+def test_graph_and_eager_reverse_passes_agree(pbf_mod, case, cuda_device):
+    """The reverse pass replays each segment as a captured CUDA graph (one per
+    segment length and starting buffer role); without graphs it launches the
+    same work eagerly.  With 10 substeps in segments of 4, 4 and 2, two graphs
+    are captured and one is replayed.  A second backward replays them all.
+    The adjoint's atomic sums make the last bits run-dependent, so the two are
+    compared within GRAD_TOL; a wrong segment or buffer role would be off by
+    far more."""
+    params, pos, vel, R, target = case
+    results = {}
+    for graph in (True, False):
+        with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+            sim.use_graph(graph)
+            sim.rollout_forward(SUBSTEPS, 4)
+            dldx = _dl_dx(sim.positions_by_id(), target)
+            first = sim.rollout_backward(dldx)
+            second = sim.rollout_backward(dldx)
+        results[graph] = (first, second)
+    for (gv, gc, gg), (ev, ec, eg) in ((results[True][0], results[False][0]), (results[True][1], results[False][0])):
+        dv, dc, dg = _rel(gv[:, :3], ev[:, :3]), abs(gc - ec) / abs(ec), _rel(gg, eg)
+        print(f"graph vs eager reverse pass: dv0 {dv:.2e}, dc {dc:.2e}, dg {dg:.2e}")
+        assert dv < GRAD_TOL and dc < GRAD_TOL and dg < GRAD_TOL
+
+
 def test_adjoint_matches_central_differences(pbf_mod, case, cuda_device):
     """Directional derivatives of the GPU gradient against central
     differences (step 1e-3) of the FP64 replay on 64 random directions."""
