@@ -462,6 +462,8 @@ def gpu_arm(args) -> None:
     sim.close()
     if dist is not None:
         dist.destroy_process_group()
+    if dist is not None:
+        dist.destroy_process_group()
 
 
 MODES = {
