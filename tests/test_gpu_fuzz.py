@@ -62,3 +62,25 @@ def test_random_configuration_bit_exact(seed, pbf_mod, oracle_mod, cuda_device):
         assert bad == 0, (f"seed {seed}: {name} differs in {bad} words "
                           f"(N {params.particleCount}, grid {params.gridBufSize}, circles {params.friendsCircles}x"
                           f"{params.particlesPerCircle}, iterations {params.simIterations}, algorithm {algorithm})")
+
+
+@pytest.mark.parametrize("seed", SEEDS)
+def test_random_configuration_relaxed_within_tolerance(seed, pbf_mod, oracle_mod, cuda_device):
+    """relaxedMath 1 on the same draws, one substep: positions within 1e-5
+    relative (max |gpu - exact| / max |exact|) of the exact oracle."""
+    params, pos, vel, _, algorithm, balance = draw(pbf_mod, seed)
+    params.relaxedMath = 1
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        sim.set_launch_shape(sim.launch_shape()[:5] + [algorithm, balance])
+        sim.Step(1)
+        gp, _, _ = sim.read_state()
+    exact = params.copy()
+    exact.relaxedMath = 0
+    op, _, _ = oracle_mod.step(exact, pos, vel, 1)
+    g, o = gp[:, :3].astype(np.float64), op[:, :3].astype(np.float64)
+    finite = np.isfinite(o).all(axis=1)
+    assert np.array_equal(finite, np.isfinite(g).all(axis=1)), f"seed {seed}: non-finite positions differ"
+    if finite.any():
+        rel = np.max(np.abs(g[finite] - o[finite])) / max(np.max(np.abs(o[finite])), 1e-30)
+        print(f"seed {seed}: relaxed vs exact, one substep: {rel:.2e}")
+        assert rel < 1e-5, f"seed {seed}: {rel:.2e}"
