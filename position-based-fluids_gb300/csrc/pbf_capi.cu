@@ -49,6 +49,7 @@ struct pbf_ctx {
     uint32_t* hist = nullptr;
     uint32_t* cells = nullptr;
     uint32_t* list = nullptr;
+    uint32_t* flat = nullptr;    // the friends of the substep in order, one flat row per position (see enqueue_substep)
     uint2* meta = nullptr;       // per-particle friend counts per circle + kept circles
     int* errWord = nullptr;
     size_t histWords = 0;
@@ -494,11 +495,13 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     for (unsigned it = 0; it < iters; ++it) {
         float4* packed = tape ? tape->q[it] : ctx->pred[a ^ 1];
         mark("computeScaling", (int)it);
-        pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, ls.scaling, ls.balance, s);
+        // the first density pass records the friends as flat rows; the passes after it walk those
+        pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, it == 0 ? nullptr : ctx->flat,
+                                    it == 0 ? ctx->flat : nullptr, ls.scaling, ls.balance, s);
         mark("computeDelta", (int)it);
         pbf::launch_compute_delta(c, b, packed, ctx->pos[sortedPos], ctx->pred[a], ctx->density, list, meta,
                                   it + 1 == iters, tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr,
-                                  ls.delta, ls.balance, s);
+                                  ctx->flat, ls.delta, ls.balance, s);
         launched += 2;
     }
     if (iters == 0) {  // packData with the density buffer as it stands (src/Simulation.cpp:591)
@@ -512,9 +515,12 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
                                   paused ? nullptr : ctx->idsTmp, ctx->ids, s);
     if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->v2, ctx->vel[V], v4, cudaMemcpyDeviceToDevice, s));
     mark("applyViscosity");
-    pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, ls.viscosity, ls.balance, s);
+    const uint32_t* flatIn = iters > 0 ? ctx->flat : nullptr;  // recorded only when a density pass ran
+    pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, flatIn, ls.viscosity,
+                                ls.balance, s);
     mark("applyVorticity");
-    pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, ls.vorticity, ls.balance, s);
+    pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, flatIn, ls.vorticity,
+                                ls.balance, s);
     launched += 3;
     if (rangeOpen) nvtxRangePop();
     PBF_CUDA(ctx, cudaGetLastError());
@@ -796,7 +802,7 @@ int pbf_destroy(pbf_ctx* ctx) {
         dev_free(ctx->keys[k]); dev_free(ctx->perm[k]);
     }
     dev_free(ctx->omega); dev_free(ctx->density); dev_free(ctx->hist); dev_free(ctx->cells);
-    dev_free(ctx->list); dev_free(ctx->meta); dev_free(ctx->errWord);
+    dev_free(ctx->list); dev_free(ctx->flat); dev_free(ctx->meta); dev_free(ctx->errWord);
     dev_free(ctx->scenes); dev_free(ctx->sceneOf); dev_free(ctx->ids); dev_free(ctx->idsTmp);
     dev_free(ctx->quadsDev); dev_free(ctx->maskDev); dev_free(ctx->waveDev);
     if (ctx->timingAnchor) cudaEventDestroy(ctx->timingAnchor);
@@ -887,7 +893,8 @@ int pbf_init_cells(pbf_ctx* ctx) {
     ctx->listSlots = (int)(p.friendsCircles * p.particlesPerCircle);
     ctx->cellsN = ctx->n;
     ++ctx->epoch;
-    if ((rc = dev_alloc(ctx, &ctx->list, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->meta, ctx->n)))
+    if ((rc = dev_alloc(ctx, &ctx->list, (size_t)ctx->listSlots * ctx->n)) ||
+        (rc = dev_alloc(ctx, &ctx->flat, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->meta, ctx->n)))
         return rc;
     PBF_CUDA(ctx, cudaMemset(ctx->meta, 0, 8 * (size_t)ctx->n));
     ctx->cellsReady = true;

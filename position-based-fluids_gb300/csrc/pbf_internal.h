@@ -101,18 +101,25 @@ void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t k
 // algorithm: LaunchShape::friendsAlgorithm
 void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
                           uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s);
+// flatIn / flatOut (may be NULL): the friends recorded in order as flat rows
+// flat[t * N + i] by the first density pass of a substep (flatOut) and read
+// from there by the passes after it (flatIn) instead of the circle rows.
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
-                            const uint32_t* list, const uint2* meta, int block, int balance, cudaStream_t s);
+                            const uint32_t* list, const uint2* meta, const uint32_t* flatIn, uint32_t* flatOut,
+                            int block, int balance, cudaStream_t s);
 // posPrev: the sorted positions, read only by the force planes.
 void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, const float4* posPrev,
                           float4* predOut, const float* density, const uint32_t* list, const uint2* meta,
-                          int lastIteration, uint8_t* clampMask, int block, int balance, cudaStream_t s);
+                          int lastIteration, uint8_t* clampMask, const uint32_t* flatIn, int block, int balance,
+                          cudaStream_t s);
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
                               float4* vel, const uint32_t* idsIn, uint32_t* idsOut, cudaStream_t s);
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
-                            float4* omega, const uint32_t* list, const uint2* meta, int block, int balance, cudaStream_t s);
+                            float4* omega, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
+                            int balance, cudaStream_t s);
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
-                            float4* velOut, const uint32_t* list, const uint2* meta, int block, int balance, cudaStream_t s);
+                            float4* velOut, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
+                            int balance, cudaStream_t s);
 
 // ---- radix sort (pbf_sort.cu) ----
 struct SortPlan {
