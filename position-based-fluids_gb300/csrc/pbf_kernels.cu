@@ -573,7 +573,7 @@ __device__ __forceinline__ float spiky_over_r(const DevConsts& c, float r2, floa
 }
 
 // compute_scaling.cl:27-112 followed by pack_data.cl (w = lambda).
-template <bool R, bool B>
+template <bool R, bool B, int W>
 __global__ void __launch_bounds__(kMaxBlock)
 compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __restrict__ predPacked,
                        float* __restrict__ density, const uint32_t* __restrict__ list,
@@ -587,7 +587,7 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
     // complete neighbour sets count the particle itself first: d = h^2 - 0
     float ds = c.complete ? c.h2 * c.h2 * c.h2 : 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
     constexpr int U = 4;
-    gather_any<U>(list, flatIn, flatOut, n, i, FriendRows(mt, kept_density(mt), c.perCircle),
+    gather_walk<W, U>(list, flatIn, flatOut, n, i, FriendRows(mt, kept_density(mt), c.perCircle),
                       [&](uint32_t j) { return __ldg(pred + checked_index(j, (uint32_t)n, c.err, kErrFriendIndex)); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         if (R) {
@@ -632,7 +632,7 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
 // the optional box clamp on `future`, then update_predicted.cl.  After the
 // last iteration w carries the density (pack_data.cl with the density source,
 // src/Simulation.cpp:591).
-template <bool R, bool B>
+template <bool R, bool B, int W>
 __global__ void __launch_bounds__(kMaxBlock)
 compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const float4* __restrict__ posPrev,
                      float4* __restrict__ predOut, const float* __restrict__ density, const uint32_t* __restrict__ list,
@@ -645,7 +645,7 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const 
     const uint64_t mt = load_meta(meta, i);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     constexpr int U = 4;
-    gather_any<U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
+    gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
                       [&](uint32_t j) { return __ldg(pp + checked_index(j, (uint32_t)n, c.err, kErrFriendIndex)); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         if (R) {
@@ -737,7 +737,7 @@ __global__ void update_velocities_kernel(DevConsts c, const float4* __restrict__
 
 // apply_viscosity.cl:12-86, every neighbour read from the pre-pass
 // velocities (Jacobi).
-template <bool R, bool B>
+template <bool R, bool B, int W>
 __global__ void __launch_bounds__(kMaxBlock)
 apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const float4* __restrict__ velIn,
                        float4* __restrict__ velOut, float4* __restrict__ omega,
@@ -750,7 +750,7 @@ apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, co
     const uint64_t mt = load_meta(meta, i);
     float vsx = 0.0f, vsy = 0.0f, vsz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
     constexpr int U = 4;
-    gather_any<U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
+    gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
                       [&](uint32_t j) { j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex); return PairRec{__ldg(pred + j), __ldg(velIn + j)}; }, [&](const PairRec& q) {
         const float4 pj = q.a;
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -793,7 +793,7 @@ apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, co
 }
 
 // apply_vorticity.cl:12-86
-template <bool R, bool B>
+template <bool R, bool B, int W>
 __global__ void __launch_bounds__(kMaxBlock)
 apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
                        const float4* __restrict__ velIn, float4* __restrict__ velOut,
@@ -806,7 +806,7 @@ apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float
     const uint64_t mt = load_meta(meta, i);
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
     constexpr int U = 4;
-    gather_any<U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
+    gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
                       [&](uint32_t j) { j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex); return PairRec{__ldg(pred + j), __ldg(omega + j)}; }, [&](const PairRec& q) {
         const float4 pj = q.a;
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -905,8 +905,16 @@ void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
                             const uint32_t* list, const uint2* meta, const uint32_t* flatIn, uint32_t* flatOut,
                             int block, int balance, cudaStream_t s) {
-    auto k = c.relaxed ? (balance ? compute_scaling_kernel<true, true> : compute_scaling_kernel<true, false>)
-                       : (balance ? compute_scaling_kernel<false, true> : compute_scaling_kernel<false, false>);
+    const int w = flatOut ? kWalkRecord : (flatIn ? kWalkFlat : kWalkRows);
+    auto pick = [w](auto rows, auto record, auto flat) { return w == kWalkFlat ? flat : (w == kWalkRecord ? record : rows); };
+    auto k = c.relaxed ? (balance ? pick(compute_scaling_kernel<true, true, kWalkRows>, compute_scaling_kernel<true, true, kWalkRecord>,
+                                         compute_scaling_kernel<true, true, kWalkFlat>)
+                                  : pick(compute_scaling_kernel<true, false, kWalkRows>, compute_scaling_kernel<true, false, kWalkRecord>,
+                                         compute_scaling_kernel<true, false, kWalkFlat>))
+                       : (balance ? pick(compute_scaling_kernel<false, true, kWalkRows>, compute_scaling_kernel<false, true, kWalkRecord>,
+                                         compute_scaling_kernel<false, true, kWalkFlat>)
+                                  : pick(compute_scaling_kernel<false, false, kWalkRows>, compute_scaling_kernel<false, false, kWalkRecord>,
+                                         compute_scaling_kernel<false, false, kWalkFlat>));
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, predPacked, density, list, meta, flatIn, flatOut);
 }
 
@@ -914,8 +922,11 @@ void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked,
                           float4* predOut, const float* density, const uint32_t* list, const uint2* meta,
                           int lastIteration, uint8_t* clampMask, const uint32_t* flatIn, int block, int balance,
                           cudaStream_t s) {
-    auto k = c.relaxed ? (balance ? compute_delta_kernel<true, true> : compute_delta_kernel<true, false>)
-                       : (balance ? compute_delta_kernel<false, true> : compute_delta_kernel<false, false>);
+    auto pick = [flatIn](auto rows, auto flat) { return flatIn ? flat : rows; };
+    auto k = c.relaxed ? (balance ? pick(compute_delta_kernel<true, true, kWalkRows>, compute_delta_kernel<true, true, kWalkFlat>)
+                                  : pick(compute_delta_kernel<true, false, kWalkRows>, compute_delta_kernel<true, false, kWalkFlat>))
+                       : (balance ? pick(compute_delta_kernel<false, true, kWalkRows>, compute_delta_kernel<false, true, kWalkFlat>)
+                                  : pick(compute_delta_kernel<false, false, kWalkRows>, compute_delta_kernel<false, false, kWalkFlat>));
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, predPacked, posPrev, predOut, density, list, meta, lastIteration,
                                                clampMask, flatIn);
 }
@@ -928,16 +939,22 @@ void launch_update_velocities(const DevConsts& c, const float4* pred, const floa
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
                             float4* omega, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
                             int balance, cudaStream_t s) {
-    auto k = c.relaxed ? (balance ? apply_viscosity_kernel<true, true> : apply_viscosity_kernel<true, false>)
-                       : (balance ? apply_viscosity_kernel<false, true> : apply_viscosity_kernel<false, false>);
+    auto pick = [flatIn](auto rows, auto flat) { return flatIn ? flat : rows; };
+    auto k = c.relaxed ? (balance ? pick(apply_viscosity_kernel<true, true, kWalkRows>, apply_viscosity_kernel<true, true, kWalkFlat>)
+                                  : pick(apply_viscosity_kernel<true, false, kWalkRows>, apply_viscosity_kernel<true, false, kWalkFlat>))
+                       : (balance ? pick(apply_viscosity_kernel<false, true, kWalkRows>, apply_viscosity_kernel<false, true, kWalkFlat>)
+                                  : pick(apply_viscosity_kernel<false, false, kWalkRows>, apply_viscosity_kernel<false, false, kWalkFlat>));
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, velIn, velOut, omega, list, meta, flatIn);
 }
 
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
                             float4* velOut, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
                             int balance, cudaStream_t s) {
-    auto k = c.relaxed ? (balance ? apply_vorticity_kernel<true, true> : apply_vorticity_kernel<true, false>)
-                       : (balance ? apply_vorticity_kernel<false, true> : apply_vorticity_kernel<false, false>);
+    auto pick = [flatIn](auto rows, auto flat) { return flatIn ? flat : rows; };
+    auto k = c.relaxed ? (balance ? pick(apply_vorticity_kernel<true, true, kWalkRows>, apply_vorticity_kernel<true, true, kWalkFlat>)
+                                  : pick(apply_vorticity_kernel<true, false, kWalkRows>, apply_vorticity_kernel<true, false, kWalkFlat>))
+                       : (balance ? pick(apply_vorticity_kernel<false, true, kWalkRows>, apply_vorticity_kernel<false, true, kWalkFlat>)
+                                  : pick(apply_vorticity_kernel<false, false, kWalkRows>, apply_vorticity_kernel<false, false, kWalkFlat>));
     k<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta, flatIn);
 }
 
