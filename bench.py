@@ -51,29 +51,33 @@ FALLBACK_HBM_GBS = 6800.0
 # neighbour records gathered through the caches are not counted).  `nl` / `nd`
 # are the mean neighbour-list lengths of the density pass / the other passes.
 STAGE_BYTES = {
-    "predictPositions": lambda nl, nd: 72.0,
-    "sortParticles": lambda nl, nd: 68.0,
-    "updateCells": lambda nl, nd: 12.0,
-    "buildFriendsList": lambda nl, nd: 20.0 + 4.0 * nl,
-    "resetPartList": lambda nl, nd: 12.0,
-    "computeScaling": lambda nl, nd: 40.0 + 4.0 * nl,
-    "computeDelta": lambda nl, nd: 40.0 + 4.0 * nd,
-    "updateVelocities": lambda nl, nd: 80.0,
-    "applyViscosity": lambda nl, nd: 68.0 + 4.0 * nd,
-    "applyVorticity": lambda nl, nd: 68.0 + 4.0 * nd,
+    "predictPositions": lambda nl, nd, it=4: 72.0,
+    "sortParticles": lambda nl, nd, it=4: 68.0,
+    "updateCells": lambda nl, nd, it=4: 12.0,
+    "buildFriendsList": lambda nl, nd, it=4: 20.0 + 4.0 * nl,
+    "resetPartList": lambda nl, nd, it=4: 12.0,
+    # per density pass: the friend entries read; the first pass of a substep
+    # also writes them as flat rows for the passes after it (it = iterations)
+    "computeScaling": lambda nl, nd, it=4: 40.0 + 4.0 * nl + 4.0 * nl / max(it, 1),
+    "computeDelta": lambda nl, nd, it=4: 40.0 + 4.0 * nd,
+    "updateVelocities": lambda nl, nd, it=4: 80.0,
+    "applyViscosity": lambda nl, nd, it=4: 68.0 + 4.0 * nd,
+    "applyVorticity": lambda nl, nd, it=4: 68.0 + 4.0 * nd,
 }
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and warp
-# instructions (smsp__inst_executed.sum) of one exact-mode launch, from ncu
-# captures of the dam_break_1m scene in the first substep of frame 51 (256-thread
-# blocks, plain thread map), with the mean list lengths of that substep (density
-# pass nl, other passes nd).  Scaled to the measured list lengths: the traffic
-# by the stage's algorithmic bytes, the instructions in proportion to the list
+# instructions (smsp__inst_executed.sum) per launch, the mean over the four
+# launches of each pass in one substep (for the density pass: the one that
+# records the flat friend rows and three that read them), from ncu captures of
+# the dam_break_1m scene in the first substep of frame 51 (256-thread blocks,
+# plain thread map), with the mean list lengths of that substep (density pass
+# nl, other passes nd).  Scaled to the measured list lengths: the traffic by
+# the stage's algorithmic bytes, the instructions in proportion to the list
 # length of the pass.
-TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 307.58e6, "nl": 38.88, "nd": 33.07},
-                   "computeDelta": {"bytes": 268.21e6, "nl": 38.88, "nd": 33.07}}
-ISSUE_CAPTURE = {"computeScaling": {"inst": 163.26e6, "nl": 38.88, "nd": 33.07},
-                 "computeDelta": {"inst": 167.33e6, "nl": 38.88, "nd": 33.07}}
+TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 311.79e6, "nl": 38.88, "nd": 33.07},
+                   "computeDelta": {"bytes": 219.73e6, "nl": 38.88, "nd": 33.07}}
+ISSUE_CAPTURE = {"computeScaling": {"inst": 152.28e6, "nl": 38.88, "nd": 33.07},
+                 "computeDelta": {"inst": 148.34e6, "nl": 38.88, "nd": 33.07}}
 SM_COUNT = 152
 SCHEDULERS_PER_SM = 4
 
@@ -372,13 +376,13 @@ def gpu_arm(args) -> None:
     dominant = max((k for k in stage_ms if k in STAGE_BYTES), key=lambda k: stage_ms[k])
     launches_per_frame = per_frame_launches.get(dominant, sub)
     launch_ms = stage_ms[dominant] / launches_per_frame
-    algo_bytes = STAGE_BYTES[dominant](nl, nd) * n
+    algo_bytes = STAGE_BYTES[dominant](nl, nd, iters) * n
     peak, peak_kind = measured_peaks()
     achieved = algo_bytes / (launch_ms / 1000.0) / 1e9
     traffic = None
     if dominant in TRAFFIC_CAPTURE:
         cap = TRAFFIC_CAPTURE[dominant]
-        scale = STAGE_BYTES[dominant](nl, nd) / STAGE_BYTES[dominant](cap["nl"], cap["nd"])
+        scale = STAGE_BYTES[dominant](nl, nd, iters) / STAGE_BYTES[dominant](cap["nl"], cap["nd"], 4)
         traffic = cap["bytes"] * scale
     issue = None
     if dominant in ISSUE_CAPTURE and args.math == "exact":
@@ -524,7 +528,7 @@ def sweep(args) -> None:
                 byts = 0.0
                 for k in names:
                     if k in STAGE_BYTES:
-                        byts += STAGE_BYTES[k](nl, nd) * n * launches.get(k, sub)
+                        byts += STAGE_BYTES[k](nl, nd, iters) * n * launches.get(k, sub)
                     elif k == "radixsort":
                         byts += (16.0 * 3 + 4.0) * n * sub  # 3 passes of 8-bit digits
                 groups[g] = {"ms_per_step": round(ms, 4), "gb_per_s": byts / (ms / 1e3) / 1e9 if ms else None,
