@@ -19,6 +19,10 @@
 //                           reference's friends layout, build_friends_list.cl:
 //                           1-21); a warp of consecutive particles reads one
 //                           row coalesced.
+//   flat                  : uint32[circles * perCircle][N]: particle i's
+//                           friends in summation order, the t-th in row t;
+//                           recorded by the first density pass of a substep
+//                           and walked by the passes after it.
 //   meta                  : uint2[N] per particle: 7-bit friend count of each
 //                           of up to 8 circles (bits 0-55), the circles the
 //                           density pass keeps (bits 56-59) and the circles
