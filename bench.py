@@ -12,14 +12,16 @@ step is one 1/60 s frame = 2 substeps of Simulation::Step.
   e2e    : the same metric through the C-ABI with host buffers, over the same
            frames (replayed from the state the timed frames started from):
            every frame copies positions + velocities in from pinned host
-           memory, steps, and copies them back out (wall clock).
+           memory, steps, and copies them back out, the positions while the
+           last substep's XSPH and vorticity run (wall clock).
   roofline: the dominant kernel's algorithmic bytes per launch over its
            average launch time (CUDA events between stages on the library's
            stream, in a separate pass of the same frames), against the
            measured HBM copy bandwidth.
 
---impl reference times the CPU restatement of the reference's pipeline
-(OpenMP over all host cores) on the same scene instead.
+--impl reference times the reference's own kernels on the host cores (its
+OpenCL C compiled through a C++ shim, OpenMP over all cores; the CPU
+restatement where they were not compiled) on the same scene instead.
 Multi-GPU (torchrun): every rank advances its own replica of the scene;
 value sums the particles of all ranks over the slowest rank's time.
 """
@@ -333,8 +335,7 @@ def gpu_arm(args) -> None:
     e2e_steps = max(1, min(args.steps, args.e2e_steps or args.steps))
     def e2e_frame():  # upload, step, download through the C-ABI; one wait per frame
         sim.write_state_async(hpos.data_ptr(), hvel.data_ptr())
-        sim.step_async(sub)
-        sim.read_state_async(hpos.data_ptr(), hvel.data_ptr())
+        sim.step_read_async(sub, hpos.data_ptr(), hvel.data_ptr())  # positions copied during XSPH/vorticity
         sim.synchronize()
 
     for _ in range(3):  # warm-up frames beyond the timed ones

@@ -193,6 +193,17 @@ int pbf_write_state(pbf_ctx* ctx, const float* pos, const float* vel);
 int pbf_write_state_async(pbf_ctx* ctx, const float* pos, const float* vel);
 int pbf_read_state_async(pbf_ctx* ctx, float* pos, float* vel, float* pred);
 
+/* pbf_step_async(substeps) followed by pbf_read_state_async(pos, vel, NULL),
+   with the same results, but the position copy overlaps the last substep:
+   positions are final after updateVelocities (update_velocities.cl), so they
+   are copied on a second stream while applyViscosity and applyVorticity run.
+   The velocity copy follows applyVorticity.  The reference's frame loop
+   (src/Runner.cpp:118-130) steps and then hands positions to the renderer;
+   this call is that frame for a host-memory consumer.  Either pointer may be
+   NULL; page-locked memory is needed for the overlap.  With stage timing on,
+   the copies follow the step. */
+int pbf_step_read_async(pbf_ctx* ctx, int substeps, float* pos, float* vel);
+
 /* Device address of the current positions (float4 x particleCount), valid
    until the next step.  Headless replacement of the GL buffer IDs
    mSharedPingBufferID / mSharedPongBufferID (src/Simulation.hpp:130-135). */

@@ -81,10 +81,23 @@ struct pbf_ctx {
     int curPos = 0, curVel = 0, curPred = 1, keysIdx = 0;
     bool stepped = false;
 
+    // pbf_step_read_async: the last substep copies its final positions out on
+    // copyStream while XSPH and vorticity run, and its velocities after them
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t evPosReady = nullptr, evCopyDone = nullptr;
+    float* readPos = nullptr;
+    float* readVel = nullptr;
+
+    // A captured substep: the plain one, and the one with pbf_step_read_async's
+    // copies (for one pair of page-locked destinations)
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        int pos = -1;          // the position buffer it starts from
+        size_t kernels = 0;    // its kernel nodes, counted as launches
+        float* host[2] = {nullptr, nullptr};
+    };
     bool useGraph = true;
-    cudaGraphExec_t graph = nullptr;
-    int graphPos = -1;
-    size_t graphNodes = 0;
+    StepGraph graph, readGraph;
     uint64_t launches = 0;
 
     bool stageTiming = false;
@@ -298,10 +311,14 @@ void apply_planes(pbf_ctx* ctx) {
 
 // The captured substep; the reverse pass's segment graphs are dropped with
 // it by drop_graph (they bake in the same constants, shapes and buffers).
+void drop_one_graph(pbf_ctx::StepGraph& g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = pbf_ctx::StepGraph{};
+}
+
 void drop_step_graph(pbf_ctx* ctx) {
-    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
-    ctx->graph = nullptr;
-    ctx->graphPos = -1;
+    drop_one_graph(ctx->graph);
+    drop_one_graph(ctx->readGraph);
 }
 
 void drop_segment_graphs(pbf_ctx* ctx) {
@@ -513,6 +530,12 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     mark("updateVelocities");
     pbf::launch_update_velocities(c, ctx->pred[a], ctx->pos[sortedPos], ctx->pos[sortedPos ^ 1], ctx->vel[V],
                                   paused ? nullptr : ctx->idsTmp, ctx->ids, s);
+    if (ctx->readPos) {  // the positions are final: copy them out while XSPH and vorticity run
+        PBF_CUDA(ctx, cudaEventRecord(ctx->evPosReady, s));
+        PBF_CUDA(ctx, cudaStreamWaitEvent(ctx->copyStream, ctx->evPosReady, 0));
+        PBF_CUDA(ctx, cudaMemcpyAsync(ctx->readPos, ctx->pos[sortedPos ^ 1], v4, cudaMemcpyDeviceToHost, ctx->copyStream));
+        PBF_CUDA(ctx, cudaEventRecord(ctx->evCopyDone, ctx->copyStream));
+    }
     if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->v2, ctx->vel[V], v4, cudaMemcpyDeviceToDevice, s));
     mark("applyViscosity");
     const uint32_t* flatIn = iters > 0 ? ctx->flat : nullptr;  // recorded only when a density pass ran
@@ -523,6 +546,8 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
                                 ls.balance, s);
     launched += 3;
     if (rangeOpen) nvtxRangePop();
+    if (ctx->readVel) PBF_CUDA(ctx, cudaMemcpyAsync(ctx->readVel, ctx->vel[V], v4, cudaMemcpyDeviceToHost, s));
+    if (ctx->readPos) PBF_CUDA(ctx, cudaStreamWaitEvent(s, ctx->evCopyDone, 0));  // later work waits for the copy
     PBF_CUDA(ctx, cudaGetLastError());
     ctx->curPos = sortedPos ^ 1;
     ctx->curPred = a;
@@ -530,8 +555,12 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     return PBF_OK;
 }
 
-int capture_graph(pbf_ctx* ctx) {
-    drop_graph(ctx);
+// Capture one substep into the plain slot, or with the copies to
+// ctx->readPos / readVel into the read slot.
+int capture_graph(pbf_ctx* ctx, bool read) {
+    pbf_ctx::StepGraph& slot = read ? ctx->readGraph : ctx->graph;
+    drop_one_graph(slot);
+    if (!read) drop_segment_graphs(ctx);
     const int savedPos = ctx->curPos, savedPred = ctx->curPred, savedKeys = ctx->keysIdx;
     const uint64_t savedLaunches = ctx->launches;
     cudaGraph_t g = nullptr;
@@ -544,13 +573,21 @@ int capture_graph(pbf_ctx* ctx) {
     ctx->launches = savedLaunches;
     if (rc != PBF_OK) { if (g) cudaGraphDestroy(g); return rc; }
     if (e != cudaSuccess) return fail(ctx, PBF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    size_t nodes = 0;
+    size_t nodes = 0, kernels = 0;
     cudaGraphGetNodes(g, nullptr, &nodes);
-    e = cudaGraphInstantiate(&ctx->graph, g, 0);
+    std::vector<cudaGraphNode_t> list(nodes);
+    if (nodes) cudaGraphGetNodes(g, list.data(), &nodes);
+    for (cudaGraphNode_t node : list) {
+        cudaGraphNodeType type;
+        if (cudaGraphNodeGetType(node, &type) == cudaSuccess && type == cudaGraphNodeTypeKernel) ++kernels;
+    }
+    e = cudaGraphInstantiate(&slot.exec, g, 0);
     cudaGraphDestroy(g);
-    if (e != cudaSuccess) { ctx->graph = nullptr; return fail(ctx, PBF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
-    ctx->graphPos = savedPos;
-    ctx->graphNodes = nodes;
+    if (e != cudaSuccess) { slot.exec = nullptr; return fail(ctx, PBF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
+    slot.pos = savedPos;
+    slot.kernels = kernels;
+    slot.host[0] = ctx->readPos;
+    slot.host[1] = ctx->readVel;
     return PBF_OK;
 }
 
@@ -806,6 +843,9 @@ int pbf_destroy(pbf_ctx* ctx) {
     dev_free(ctx->scenes); dev_free(ctx->sceneOf); dev_free(ctx->ids); dev_free(ctx->idsTmp);
     dev_free(ctx->quadsDev); dev_free(ctx->maskDev); dev_free(ctx->waveDev);
     if (ctx->timingAnchor) cudaEventDestroy(ctx->timingAnchor);
+    if (ctx->evPosReady) cudaEventDestroy(ctx->evPosReady);
+    if (ctx->evCopyDone) cudaEventDestroy(ctx->evCopyDone);
+    if (ctx->copyStream) cudaStreamDestroy(ctx->copyStream);
     free_render(ctx);
     free_rollout(ctx);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1204,19 +1244,67 @@ int pbf_step_async(pbf_ctx* ctx, int substeps) {
     for (int k = 0; k < substeps; ++k) {
         const bool graphOk = ctx->useGraph && !ctx->paused && !ctx->stageTiming;
         if (graphOk) {
-            if (!ctx->graph || ctx->graphPos != ctx->curPos)
-                if ((rc = capture_graph(ctx))) return rc;
-            PBF_CUDA(ctx, cudaGraphLaunch(ctx->graph, ctx->stream));
+            if (!ctx->graph.exec || ctx->graph.pos != ctx->curPos)
+                if ((rc = capture_graph(ctx, false))) return rc;
+            PBF_CUDA(ctx, cudaGraphLaunch(ctx->graph.exec, ctx->stream));
             // the replayed substep has the captured buffer roles
             ctx->keysIdx = ctx->plan.passes & 1;
             ctx->curPred = 1;
-            ctx->launches += ctx->graphNodes;
+            ctx->launches += ctx->graph.kernels;
         } else {
             if ((rc = enqueue_substep(ctx, ctx->stageTiming ? &clock : nullptr))) return rc;
         }
         ctx->stepped = true;
     }
     if (ctx->stageTiming) return clock.finish();
+    return PBF_OK;
+}
+
+bool page_locked(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return a.type == cudaMemoryTypeHost;
+}
+
+int pbf_step_read_async(pbf_ctx* ctx, int substeps, float* pos, float* vel) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (substeps < 1) return fail(ctx, PBF_ERR_INVALID, "pbf_step_read_async: substeps must be >= 1");
+    if (ctx->stageTiming) {  // the trackers time whole substeps: no overlap
+        if ((rc = pbf_step_async(ctx, substeps))) return rc;
+        return pbf_read_state_async(ctx, pos, vel, nullptr);
+    }
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (substeps > 1 && (rc = pbf_step_async(ctx, substeps - 1))) return rc;
+    if (pos) {
+        if (!ctx->copyStream) PBF_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copyStream, cudaStreamNonBlocking));
+        if (!ctx->evPosReady) PBF_CUDA(ctx, cudaEventCreateWithFlags(&ctx->evPosReady, cudaEventDisableTiming));
+        if (!ctx->evCopyDone) PBF_CUDA(ctx, cudaEventCreateWithFlags(&ctx->evCopyDone, cudaEventDisableTiming));
+    }
+    ctx->readPos = pos;
+    ctx->readVel = vel;
+    // the last substep with its copies: a captured graph when both
+    // destinations are page-locked (a graph's copy nodes keep their addresses)
+    const bool graphOk = ctx->useGraph && !ctx->paused && (!pos || page_locked(pos)) && (!vel || page_locked(vel));
+    if (graphOk) {
+        pbf_ctx::StepGraph& g = ctx->readGraph;
+        if (!g.exec || g.pos != ctx->curPos || g.host[0] != pos || g.host[1] != vel) rc = capture_graph(ctx, true);
+        if (rc == PBF_OK) {
+            const cudaError_t e = cudaGraphLaunch(g.exec, ctx->stream);
+            if (e != cudaSuccess) rc = fail(ctx, PBF_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(e));
+        }
+        if (rc == PBF_OK) {  // the replayed substep has the captured buffer roles, as in pbf_step_async
+            ctx->keysIdx = ctx->plan.passes & 1;
+            ctx->curPred = 1;
+            ctx->launches += g.kernels;
+        }
+    } else {
+        rc = enqueue_substep(ctx, nullptr);
+    }
+    ctx->readPos = nullptr;
+    ctx->readVel = nullptr;
+    if (rc) return rc;
+    ctx->stepped = true;
     return PBF_OK;
 }
 

@@ -129,6 +129,7 @@ def library() -> ctypes.CDLL:
         "pbf_write_state": [c_void_p, c_void_p, c_void_p],
         "pbf_write_state_async": [c_void_p, c_void_p, c_void_p],
         "pbf_read_state_async": [c_void_p, c_void_p, c_void_p, c_void_p],
+        "pbf_step_read_async": [c_void_p, c_int, c_void_p, c_void_p],
         "pbf_device_positions": [c_void_p, POINTER(c_void_p)],
         "pbf_get_stream": [c_void_p, POINTER(c_void_p)],
         "pbf_sort_state": [c_void_p, f32p, u32p, u32p, u32p],
@@ -358,6 +359,11 @@ class Simulation:
     def read_state_async(self, pos_ptr: int | None, vel_ptr: int | None = None, pred_ptr: int | None = None) -> None:
         _check(self.lib.pbf_read_state_async(self._ctx, pos_ptr, vel_ptr, pred_ptr), self._ctx)
 
+    def step_read_async(self, substeps: int, pos_ptr: int | None, vel_ptr: int | None = None) -> None:
+        """Step and copy positions / velocities to host addresses; the
+        position copy overlaps the last substep's XSPH and vorticity."""
+        _check(self.lib.pbf_step_read_async(self._ctx, substeps, pos_ptr, vel_ptr), self._ctx)
+
     def write_state_from(self, pos_ptr: int | None, vel_ptr: int | None = None) -> None:
         _check(self.lib.pbf_write_state(self._ctx, pos_ptr, vel_ptr), self._ctx)
 
@@ -509,7 +515,7 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_read_ids", "pbf_rollout_forward", "pbf_rollout_backward", "pbf_set_force_quads",
         "pbf_set_wave_position", "pbf_wave_position", "pbf_save_state", "pbf_load_state",
         "pbf_perf_trackers", "pbf_perf_export_json", "pbf_render_camera", "pbf_render_frame", "pbf_render_read",
-        "pbf_write_state_async", "pbf_read_state_async", "pbf_enable_nvtx", "pbf_load_scene", "pbf_scene_positions",
+        "pbf_write_state_async", "pbf_read_state_async", "pbf_step_read_async", "pbf_enable_nvtx", "pbf_load_scene", "pbf_scene_positions",
     ])
 
 

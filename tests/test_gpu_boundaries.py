@@ -113,6 +113,54 @@ def test_async_state_copies_match_sync(pbf_mod, cuda_device):
         assert _same(p, hp.numpy()) and _same(v, hv.numpy())
 
 
+@pytest.mark.parametrize("mode", ["graph", "eager", "pageable", "paused", "stage_timing"])
+def test_step_read_async_matches_step_then_read(pbf_mod, cuda_device, mode):
+    """pbf_step_read_async (the position copy overlapping the last substep's
+    XSPH and vorticity) against pbf_step + pbf_read_state, frame by frame:
+    page-locked buffers replay a captured substep with its copies (swapping
+    the buffers recaptures it); pageable buffers, graphs off, a paused
+    simulation and stage timing take the eager path.  The launch count grows
+    as pbf_step_async's does."""
+    torch = pytest.importorskip("torch")
+    params, pos, vel = pbf_mod.make_scene("dam_break_32k")
+    n = len(pos)
+    if mode == "pageable":
+        bufs = [(np.empty((n, 4), np.float32), np.empty((n, 4), np.float32)) for _ in range(2)]
+        ptrs = [(p.ctypes.data, v.ctypes.data) for p, v in bufs]
+        views = [(p, v) for p, v in bufs]
+    else:
+        bufs = [(torch.empty((n, 4), dtype=torch.float32).pin_memory(),
+                 torch.empty((n, 4), dtype=torch.float32).pin_memory()) for _ in range(2)]
+        ptrs = [(p.data_ptr(), v.data_ptr()) for p, v in bufs]
+        views = [(p.numpy(), v.numpy()) for p, v in bufs]
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as a, \
+         pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as b:
+        for sim in (a, b):
+            if mode == "eager":
+                sim.use_graph(False)
+            if mode == "paused":
+                sim.bPauseSim = True
+            if mode == "stage_timing":
+                sim.enable_stage_timing(True)
+        for frame, (sub, k) in enumerate([(1, 0), (2, 0), (2, 0), (3, 1), (2, 0)]):
+            la, lb = a.launch_count(), b.launch_count()
+            a.step_async(sub)
+            a.synchronize()
+            pa, va, _ = a.read_state()
+            b.step_read_async(sub, *ptrs[k])
+            b.synchronize()
+            assert _same(pa, views[k][0]) and _same(va, views[k][1]), f"frame {frame}"
+            assert b.launch_count() - lb == a.launch_count() - la
+        pb, vb, _ = b.read_state()
+        assert _same(pa, pb) and _same(va, vb)
+        b.step_read_async(1, ptrs[0][0], None)  # positions only
+        a.Step(1)
+        b.synchronize()
+        assert _same(a.read_state()[0], views[0][0])
+        with pytest.raises(pbf_mod.PbfError):
+            b.step_read_async(0, *ptrs[0])
+
+
 def test_non_finite_injection_matches_oracle(pbf_mod, oracle_mod, cuda_device):
     """A NaN and an infinite particle written into the state: the pipeline
     runs on, identically to the oracle (NaN compared as NaN), and the error
