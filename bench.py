@@ -166,38 +166,73 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_reference_sample(params, pos, vel, seconds: float, max_substeps: int | None = None) -> tuple[float, dict]:
+def stage_roofline(sim, n: int, iters: int, sub: int, frames: int, peak: float, peak_kind: str):
+    """Per-stage device times of `frames` eager frames (events between
+    stages) and the roofline of the dominant neighbour kernel: its
+    algorithmic bytes per launch (with the current mean list lengths) over
+    its mean launch time.  Returns (nl, nd, stage_ms, dominant, launch_ms,
+    roofline dict)."""
+    counts, _ = sim.read_friends(slots=1)
+    nl, nd = float(counts[:, 0].mean()), float(counts[:, 1].mean())
+    sim.enable_stage_timing(True)
+    totals: dict[str, float] = {}
+    for _ in range(frames):
+        sim.Step(sub)
+        for k, v in sim.stage_timings().items():
+            totals[k] = totals.get(k, 0.0) + v
+    sim.enable_stage_timing(False)
+    per_frame_launches = {"computeScaling": iters * sub, "computeDelta": iters * sub}
+    stage_ms = {k: v / frames for k, v in totals.items()}
+    dominant = max((k for k in stage_ms if k in STAGE_BYTES), key=lambda k: stage_ms[k])
+    launch_ms = stage_ms[dominant] / per_frame_launches.get(dominant, sub)
+    algo_bytes = STAGE_BYTES[dominant](nl, nd, iters) * n
+    achieved = algo_bytes / (launch_ms / 1000.0) / 1e9
+    traffic = None
+    if dominant in TRAFFIC_CAPTURE:
+        cap = TRAFFIC_CAPTURE[dominant]
+        traffic = cap["bytes"] * STAGE_BYTES[dominant](nl, nd, iters) / STAGE_BYTES[dominant](cap["nl"], cap["nd"], 4)
+    roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+            "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": launch_ms}
+    return nl, nd, stage_ms, dominant, launch_ms, roof
+
+
+def cpu_reference_sample(params, pos, vel, seconds: float, max_substeps: int | None = None,
+                         warmup: int = 1) -> tuple[float, dict]:
     """Time the reference's CPU path on a bounded sample of the scene: the
     reference's own kernels through the OpenCL-C shim (oracle/_ref) on all host
     threads where they were compiled, else the CPU restatement (the oracle
-    port, bit-identical to them).  Returns (particle-iterations/s, the
-    cpu_baseline fields kind / cores / sample / substeps / seconds)."""
+    port, bit-identical to them).  `warmup` (at least 1) untimed substeps
+    come first.  Returns (particle-iterations/s, the cpu_baseline fields kind /
+    cores / sample / substeps / seconds / warmup)."""
     from oracle import oracle
     n, iters = int(params.particleCount), int(params.simIterations)
+    w = max(1, int(warmup))
     if oracle.ref_available():
         try:
-            # a 1-substep run and a (k+1)-substep run: their difference is k
-            # substeps, the buffer setup of each run cancels
+            # a w-substep run and a (w+k)-substep run from the same state:
+            # their difference is k substeps after w warm-up substeps, and the
+            # buffer setup of each run cancels
             t0 = time.perf_counter()
-            oracle.ref_step(params, pos, vel, 1, threads=0)
-            one = time.perf_counter() - t0
+            oracle.ref_step(params, pos, vel, w, threads=0)
+            tw = time.perf_counter() - t0
             threads = oracle.ref_max_threads()
-            k = max(1, int(seconds / max(one, 1e-3)))
+            k = max(1, int(seconds / max(tw / w, 1e-3)))
             if max_substeps:
                 k = min(k, max_substeps)
             t0 = time.perf_counter()
-            oracle.ref_step(params, pos, vel, k + 1, threads=0)
-            el = max(time.perf_counter() - t0 - one, 1e-9)
+            oracle.ref_step(params, pos, vel, w + k, threads=0)
+            el = max(time.perf_counter() - t0 - tw, 1e-9)
             return n * iters * k / el, {
-                "kind": "reference", "cores": threads, "substeps": k, "seconds": el,
-                "sample": f"{k} substep(s) of the {n}-particle scene from its initial state through the reference's "
-                          f"own kernels (OpenCL-C shim, work-items on {threads} threads): a {k + 1}-substep run "
-                          f"less a 1-substep run, {el:.1f} s"}
+                "kind": "reference", "cores": threads, "substeps": k, "seconds": el, "warmup": w,
+                "sample": f"{k} substep(s) of the {n}-particle scene after {w} warm-up substep(s) from its initial "
+                          f"state, through the reference's own kernels (OpenCL-C shim, work-items on {threads} "
+                          f"threads): a {w + k}-substep run less a {w}-substep run, {el:.1f} s"}
         except (OSError, RuntimeError, FileNotFoundError):
             pass  # no compiler or no generated unit here: the restatement below
     threads = oracle.max_threads()
+    p, v, _ = oracle.step(params, pos, vel, w, threads=threads)
     done, t0 = 0, time.perf_counter()
-    p, v = pos, vel
     while True:
         p, v, _ = oracle.step(params, p, v, 1, threads=threads)
         done += 1
@@ -205,9 +240,9 @@ def cpu_reference_sample(params, pos, vel, seconds: float, max_substeps: int | N
         if el >= seconds or (max_substeps and done >= max_substeps):
             break
     return n * iters * done / el, {
-        "kind": "port", "cores": threads, "substeps": done, "seconds": el,
-        "sample": f"{done} substep(s) of the {n}-particle scene from its initial state through the CPU restatement, "
-                  f"{el:.1f} s"}
+        "kind": "port", "cores": threads, "substeps": done, "seconds": el, "warmup": w,
+        "sample": f"{done} substep(s) of the {n}-particle scene after {w} warm-up substep(s) from its initial "
+                  f"state, through the CPU restatement, {el:.1f} s"}
 
 
 def cpu_baseline(params, pos, vel, seconds: float) -> dict:
@@ -228,11 +263,12 @@ def reference_arm(args) -> None:
     import pbf
     params, pos, vel = pbf.make_scene(args.scene)
     n, iters = int(params.particleCount), int(params.simIterations)
-    value, info = cpu_reference_sample(params, pos, vel, args.cpu_budget, max_substeps=args.steps)
+    value, info = cpu_reference_sample(params, pos, vel, args.cpu_budget, max_substeps=args.steps,
+                                       warmup=args.warmup)
     done, el = info["substeps"], info["seconds"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": done, "warmup": 1, "ms_per_step": 1000.0 * el / done,
+        "steps": done, "warmup": info["warmup"], "ms_per_step": 1000.0 * el / done,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload_name(args.scene, n, iters, int(params.subSteps)),
                    "reference_step": "one substep per timed step (a bounded sample of the frame)",
@@ -362,29 +398,9 @@ def gpu_arm(args) -> None:
                      "note": "|rho / rho0 - 1| per particle, density of the last solver iteration"}
 
     # ---- per-stage device times (eager launches, events between stages) ----
-    counts, _ = sim.read_friends(slots=1)
-    nl, nd = float(counts[:, 0].mean()), float(counts[:, 1].mean())
-    sim.enable_stage_timing(True)
-    frames = max(1, min(args.steps, 20))
-    totals: dict[str, float] = {}
-    for _ in range(frames):
-        sim.Step(sub)
-        for k, v in sim.stage_timings().items():
-            totals[k] = totals.get(k, 0.0) + v
-    sim.enable_stage_timing(False)
-    per_frame_launches = {"computeScaling": iters * sub, "computeDelta": iters * sub}
-    stage_ms = {k: v / frames for k, v in totals.items()}
-    dominant = max((k for k in stage_ms if k in STAGE_BYTES), key=lambda k: stage_ms[k])
-    launches_per_frame = per_frame_launches.get(dominant, sub)
-    launch_ms = stage_ms[dominant] / launches_per_frame
-    algo_bytes = STAGE_BYTES[dominant](nl, nd, iters) * n
     peak, peak_kind = measured_peaks()
-    achieved = algo_bytes / (launch_ms / 1000.0) / 1e9
-    traffic = None
-    if dominant in TRAFFIC_CAPTURE:
-        cap = TRAFFIC_CAPTURE[dominant]
-        scale = STAGE_BYTES[dominant](nl, nd, iters) / STAGE_BYTES[dominant](cap["nl"], cap["nd"], 4)
-        traffic = cap["bytes"] * scale
+    nl, nd, stage_ms, dominant, launch_ms, roof = stage_roofline(sim, n, iters, sub, max(1, min(args.steps, 20)),
+                                                                 peak, peak_kind)
     issue = None
     if dominant in ISSUE_CAPTURE and args.math == "exact":
         cap = ISSUE_CAPTURE[dominant]
@@ -415,9 +431,13 @@ def gpu_arm(args) -> None:
         o1.record(stream)
         o1.synchronize()
         other_ms = o0.elapsed_time(o1) / args.steps
+        *_, other_stages, _, _, other_roof = stage_roofline(sim, n, iters, sub, max(1, min(args.steps, 10)), peak,
+                                                            peak_kind)
         other_line = {"mode": other, "value": n * iters * sub / (other_ms / 1000.0), "ms_per_step": other_ms,
                       "blocks": dict(zip(["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm",
-                                          "balance"], other_blocks))}
+                                          "balance"], other_blocks)),
+                      "roofline": other_roof,
+                      "stage_ms_per_step": {k: round(v, 4) for k, v in sorted(other_stages.items(), key=lambda kv: -kv[1])}}
         sim.set_params(params)
         sim.set_launch_shape(blocks)
 
@@ -447,9 +467,7 @@ def gpu_arm(args) -> None:
                 "steps": e2e_steps, "frames": "the timed frames replayed from their start state",
                 "replay_bit_identical": e2e_replay_identical},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_ms": launch_ms},
+        "roofline": roof,
         "pipeline_roofline": {"bytes_per_particle_substep": 444.0 + 56.0 * iters, "achieved": pipeline_gbs,
                               "frac": pipeline_gbs / peak},
         **({"issue_roofline": issue} if issue else {}),

@@ -39,7 +39,8 @@ def test_reference_arm_prints_the_contract_line():
     import json
     import subprocess
     run = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--scene", "dam_break_32k",
-                          "--steps", "2", "--cpu-budget", "1"], capture_output=True, text=True, timeout=600)
+                          "--steps", "2", "--warmup", "3", "--cpu-budget", "1"], capture_output=True, text=True,
+                         timeout=600)
     assert run.returncode == 0, run.stderr[-2000:]
     lines = [l for l in run.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
@@ -49,3 +50,4 @@ def test_reference_arm_prints_the_contract_line():
         assert key in line, key
     assert line["cpu_baseline"]["kind"] in ("reference", "port") and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert line["warmup"] == 3 and 1 <= line["steps"] <= 2  # untimed warm-up substeps, then the timed ones
