@@ -79,6 +79,8 @@ def scene(pbf, dims, base="dam_break_32k", spacing=0.05, origin=(0.025,) * 3, ji
     dict(dims=(16, 16, 16), gridBufSize=64),      # hash collisions
     dict(dims=(16, 16, 16), gridBufSize=1000),    # modulo, not a power of two
     dict(dims=(2, 1, 1)),                         # two particles
+    dict(dims=(12, 12, 12), origin=(-0.3,) * 3),  # negative coordinates: cells truncate toward zero
+    dict(dims=(8, 8, 8), origin=(102.2, 0.025, 0.025)),  # x cells past 1023: Morton bits wrap
 ])
 def test_sort_and_cells_bit_exact(case, pbf_mod, oracle_mod, cuda_device):
     case = dict(case)
@@ -138,6 +140,12 @@ SUBSTEP_CASES = {
     "seven_circles_saturated": (dict(dims=(16, 16, 16), friendsCircles=7, particlesPerCircle=3), 2),
     "two_particles": (dict(dims=(2, 1, 1)), 3),
     "one_particle": (dict(dims=(1, 1, 1)), 2),
+    # unclamped blocks where the reference's cell arithmetic is at its edges:
+    # straddling the origin (cell 0 spans (-h, h), the -1 neighbours' Morton
+    # bits come from negative integers) and past 1024 cells along x (the
+    # 10-bit Morton coordinates wrap, so distant cells share hashes)
+    "across_origin": (dict(dims=(12, 12, 12), origin=(-0.3,) * 3, boxClamp=0), 3),
+    "beyond_morton_range": (dict(dims=(8, 8, 8), origin=(102.2, 0.025, 0.025), boxClamp=0), 3),
 }
 
 
