@@ -289,7 +289,7 @@ int pbf_use_graph(pbf_ctx* ctx, int enable);
    fixed working array it keeps on every GPU that loads this library (held
    until the process exits). */
 #define PBF_NOALLOC_MAX_KEYS       (1u << 20)
-#define PBF_NOALLOC_SCRATCH_BYTES  8651776u   /* 8.25 MiB */
+#define PBF_NOALLOC_SCRATCH_BYTES  8913920u   /* 8.5 MiB + 1 KiB */
 
 /* The key / sort / cell-table stage of pbf_sort_state for callers that may
    not allocate device memory: hosts that reserve all device memory at start-up

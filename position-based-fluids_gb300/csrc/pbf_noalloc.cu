@@ -26,8 +26,8 @@
 namespace {
 
 constexpr size_t kMaxKeys = PBF_NOALLOC_MAX_KEYS;
-constexpr size_t kTileKeys = 4096;  // keys per radix-sort tile above 2^18 keys; the 1024-key tiles of smaller
-                                    // sorts (pbf_sort.cu) need at most as many histograms (2^18 / 1024 = 256)
+constexpr size_t kTileKeys = 2048;  // keys per radix-sort tile from 2^18 to 2^21 keys; the 1024-key tiles of
+                                    // smaller sorts (pbf_sort.cu) need fewer histograms (2^18 / 1024 = 256)
 constexpr size_t kHistWords = 256 * (kMaxKeys / kTileKeys) + 256;  // a 256-bin histogram per tile + digit totals
 constexpr size_t kScratchWords = 2 * kMaxKeys + kHistWords;   // keys + permutation ping-pong, histograms
 static_assert(kScratchWords * 4 == PBF_NOALLOC_SCRATCH_BYTES, "scratch size stated in pbf_capi.h");

@@ -13,10 +13,11 @@
 //               totals
 //   downsweep : per-warp stable ranking with __match_any_sync and per-warp
 //               digit counters in shared memory, then the scatter.
-// A tile is 8 warps x kRounds rounds of 32 keys: 4096 keys (16 rounds), or
-// 1024 (4 rounds) at most 2^18 keys, where 4096-key tiles would leave most
-// SMs idle.  Each warp owns consecutive keys taken round by round, so
-// (warp, round, lane) order is input order.
+// A tile is 8 warps x kRounds rounds of 32 keys: 4096 keys (16 rounds) above
+// 2^21 keys, 2048 (8 rounds) above 2^18 and 1024 (4 rounds) below, so that
+// smaller sorts still spread over the SMs (at 2^20 keys, 512 tiles sort
+// 12 % faster than 256).  Each warp owns consecutive keys taken round by
+// round, so (warp, round, lane) order is input order.
 
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -29,6 +30,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kSmallSortKeys = 1 << 18;     // at most this many keys: 4-round tiles
+constexpr int kMidSortKeys = 1 << 21;       // at most this many keys: 8-round tiles
 
 template <int kRounds>
 __global__ void __launch_bounds__(kThreads)
@@ -164,7 +166,7 @@ SortPlan make_sort_plan(int n, uint32_t gridBufSize) {
     int bits = 0;
     while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)gridBufSize) ++bits;  // keys <= gridBufSize-1
     p.passes = (bits + 7) / 8;
-    p.rounds = n <= kSmallSortKeys ? 4 : 16;
+    p.rounds = n <= kSmallSortKeys ? 4 : (n <= kMidSortKeys ? 8 : 16);
     const int tile = kThreads * p.rounds;
     p.tiles = (n + tile - 1) / tile;
     p.histWords = (size_t)256 * p.tiles + 256;  // per-tile histograms, then the 256 digit totals
@@ -181,11 +183,17 @@ int launch_radix_sort(const SortPlan& plan, uint32_t* keys[2], uint32_t* perm[2]
         const int shift = 8 * pass;
         if (plan.rounds == 4)
             radix_upsweep_kernel<4><<<plan.tiles, kThreads, 0, s>>>(keys[cur], plan.n, shift, plan.tiles, hist);
+        else if (plan.rounds == 8)
+            radix_upsweep_kernel<8><<<plan.tiles, kThreads, 0, s>>>(keys[cur], plan.n, shift, plan.tiles, hist);
         else
             radix_upsweep_kernel<16><<<plan.tiles, kThreads, 0, s>>>(keys[cur], plan.n, shift, plan.tiles, hist);
         radix_scan_kernel<<<256, kThreads, 0, s>>>(hist, plan.tiles, totals);
         if (plan.rounds == 4)
             radix_downsweep_kernel<4><<<plan.tiles, kThreads, 0, s>>>(keys[cur], perm[cur], keys[cur ^ 1],
+                                                                      perm[cur ^ 1], plan.n, shift, plan.tiles, hist,
+                                                                      totals);
+        else if (plan.rounds == 8)
+            radix_downsweep_kernel<8><<<plan.tiles, kThreads, 0, s>>>(keys[cur], perm[cur], keys[cur ^ 1],
                                                                       perm[cur ^ 1], plan.n, shift, plan.tiles, hist,
                                                                       totals);
         else
