@@ -73,6 +73,25 @@ def test_autotune_keeps_results_and_state(pbf_mod, cuda_device):
             assert _same(x, y)
 
 
+def test_batch_step_read_async_matches_step_then_read(pbf_mod, cuda_device):
+    """The overlapped step-and-read-back on a batch: the same state as
+    stepping and reading after, frame by frame, with the read graph reused."""
+    torch = pytest.importorskip("torch")
+    scenes, positions = pbf_mod.make_batch_scenes(first=8)
+    pos = np.concatenate(positions)
+    n = len(pos)
+    hp = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    hv = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    with pbf_mod.Simulation.create(scenes, pos, np.zeros_like(pos), device=cuda_device) as a, \
+         pbf_mod.Simulation.create(scenes, pos, np.zeros_like(pos), device=cuda_device) as b:
+        for _ in range(3):
+            a.Step(2)
+            pa, va, _ = a.read_state()
+            b.step_read_async(2, hp.data_ptr(), hv.data_ptr())
+            b.synchronize()
+            assert _same(pa, hp.numpy()) and _same(va, hv.numpy())
+
+
 def test_batch_rejects_incompatible_scenes(pbf_mod, cuda_device):
     scenes, _ = pbf_mod.make_batch_scenes(first=2)
     scenes[1].epsilon = 123.0
