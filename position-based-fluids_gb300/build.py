@@ -100,16 +100,20 @@ def build(force: bool = False, verbose: bool = False, checked: bool = False) -> 
     if jobs:
         with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
             results = list(ex.map(lambda j: _run(j[2]), jobs))
-        for (src, _, cmd), (rc, out) in zip(jobs, results):
-            if verbose and out:
-                sys.stderr.write(out)
+        for (src, _, cmd), (rc, log) in zip(jobs, results):
+            if verbose and log:
+                sys.stderr.write(log)
             if rc != 0:
-                sys.stderr.write(out)
+                sys.stderr.write(log)
                 raise RuntimeError(f"compile failed: {src.name}\n{' '.join(cmd)}")
     objs = [str(o) for _, o, _ in compile_commands(checked)]
     if force or jobs or not lib.exists():
+        # the library exports the C-ABI (pbf_*) and nothing of its internals
+        exports = out / "exports.map"
+        exports.write_text("{\n  global: pbf_*;\n  local: *;\n};\n")
         tmp = lib.with_suffix(".so.tmp")
-        rc, log = _run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart"])
+        rc, log = _run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart",
+                        "-Xlinker", f"--version-script={exports}"])
         if rc != 0:
             sys.stderr.write(log)
             raise RuntimeError("link failed")

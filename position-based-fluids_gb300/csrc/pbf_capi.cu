@@ -769,6 +769,13 @@ int run_segment_graph(pbf_ctx* ctx, int len, pbf::AdjointBuffers& ab) {
     }
     return PBF_OK;
 }
+
+// Host memory the driver has page-locked (allocated or registered by CUDA)
+bool page_locked(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return a.type == cudaMemoryTypeHost;
+}
 }  // namespace
 
 // ================================================================ C-ABI ==
@@ -1258,12 +1265,6 @@ int pbf_step_async(pbf_ctx* ctx, int substeps) {
     }
     if (ctx->stageTiming) return clock.finish();
     return PBF_OK;
-}
-
-bool page_locked(const void* p) {
-    cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
-    return a.type == cudaMemoryTypeHost;
 }
 
 int pbf_step_read_async(pbf_ctx* ctx, int substeps, float* pos, float* vel) {

@@ -28,6 +28,20 @@ def test_every_declared_symbol_is_exported(built_lib, pbf_mod):
     assert set(pbf_mod.EXPORTED_SYMBOLS) <= declared
 
 
+def test_library_exports_only_the_declared_c_abi(built_lib):
+    """The dynamic symbol table holds exactly the functions include/*.h
+    declares: no internal C++ function or helper leaks into a caller's
+    namespace."""
+    import shutil
+    import subprocess
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    out = subprocess.run([nm, "-D", "--defined-only", str(built_lib)], capture_output=True, text=True, check=True)
+    exported = {line.split()[-1] for line in out.stdout.splitlines() if line.strip()}
+    assert exported == declared_functions()
+
+
 def test_checked_build_exports_the_same_symbols():
     """The bounds-checked build (build.py --checked) is a drop-in for the plain
     library: built from the same sources with -DPBF_CHECK_BOUNDS into its own
