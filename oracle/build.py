@@ -9,8 +9,9 @@ Two libraries:
   src/Simulation.cpp:103-127, without logging.cl) compiled as C++ through
   ``clshim.hpp`` and driven by ``ref_driver.inc``.  The generated translation
   unit ``oracle/_ref/ref_kernels.cpp`` is written from the reference checkout
-  when it is present; the only edit made to the kernel text is the rewrite of
-  OpenCL vector literals ``(float3)(a, b, c)`` into ``make_float3(a, b, c)``.
+  named by ``PBF_REFERENCE_DIR`` (or ``--reference DIR``) when it is set;
+  the only edit made to the kernel text is the rewrite of OpenCL vector
+  literals ``(float3)(a, b, c)`` into ``make_float3(a, b, c)``.
   Where the checkout is absent but a generated unit is already there, that
   unit is compiled.
 
@@ -31,7 +32,15 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE = Path(os.environ.get("PBF_REFERENCE_DIR", "/root/reference"))
+
+
+def reference_dir() -> Path | None:
+    """The reference checkout whose kernels build_ref compiles: the directory
+    named by PBF_REFERENCE_DIR, or None when it is unset (the generated unit
+    already under oracle/_ref, if any, is compiled instead)."""
+    d = os.environ.get("PBF_REFERENCE_DIR")
+    return Path(d) if d else None
+
 
 ORACLE_LIB = BUILD / "libpbf_oracle.so"
 REF_LIB = REF_OUT / "libpbf_ref.so"
@@ -76,7 +85,10 @@ def build_oracle(force: bool = False) -> Path:
 
 def generate_ref_tu() -> bool:
     """Write oracle/_ref/ref_kernels.cpp from the reference checkout."""
-    kdir = REFERENCE / "assets" / "kernels"
+    ref = reference_dir()
+    if ref is None:
+        return False
+    kdir = ref / "assets" / "kernels"
     if not kdir.is_dir():
         return False
     parts = [
@@ -117,5 +129,8 @@ def build(force: bool = False) -> None:
 
 
 if __name__ == "__main__":
+    # python oracle/build.py [--force] [--reference DIR]
+    if "--reference" in sys.argv:
+        os.environ["PBF_REFERENCE_DIR"] = sys.argv[sys.argv.index("--reference") + 1]
     build(force="--force" in sys.argv)
     print(ORACLE_LIB, REF_LIB if REF_LIB.exists() else "(reference kernels unavailable)")

@@ -65,7 +65,8 @@ def lib() -> ctypes.CDLL:
 
 
 def ref_available() -> bool:
-    return _build.REF_LIB.exists() or _build.REF_TU.exists() or (_build.REFERENCE / "assets").is_dir()
+    ref = _build.reference_dir()
+    return _build.REF_LIB.exists() or _build.REF_TU.exists() or (ref is not None and (ref / "assets").is_dir())
 
 
 def ref() -> ctypes.CDLL:

@@ -11,7 +11,8 @@ checkout), on seeded dam-break scenes and writes
 * small_case.npz — every output array of the smallest case in full.
 
 The box clamp is a stage the reference does not have, so every case runs with
-BoxClamp 0.  Run from the repository root:  python tests/golden/make_golden.py
+BoxClamp 0.  Run from the repository root, with PBF_REFERENCE_DIR naming the
+reference checkout:  PBF_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -62,7 +63,7 @@ FORCE_CASE = {"name": "force_planes_4k_4sub", "block": [16, 16, 16], "origin": [
 def reference_force_quads():
     """The 14 planes hard-coded in the reference (compute_delta.cl:169-182)."""
     import re
-    src = (oracle._build.REFERENCE / "assets" / "kernels" / "compute_delta.cl").read_text()
+    src = (oracle._build.reference_dir() / "assets" / "kernels" / "compute_delta.cl").read_text()
     vec = r"\(float3\)\(\s*([-0-9.eE]+),\s*([-0-9.eE]+),\s*([-0-9.eE]+)\)"
     pat = re.compile(r"BouncePointQuad\(positions\[i\]\.xyz, future, " + vec + r", " + vec + r", " + vec +
                      r", surfacesMask, (\d+), (\d+), edgeOffset\)")
@@ -128,8 +129,8 @@ def digest(a: np.ndarray) -> str:
 
 
 def main() -> None:
-    if not oracle.ref_available():
-        raise SystemExit("the reference checkout is needed to generate the golden vectors")
+    if oracle._build.reference_dir() is None or not oracle.ref_available():
+        raise SystemExit("set PBF_REFERENCE_DIR to the reference checkout to generate the golden vectors")
     manifest = {
         "generator": "tests/golden/make_golden.py",
         "source": "reference assets/kernels/*.cl compiled through oracle/clshim.hpp (oracle/_ref)",
