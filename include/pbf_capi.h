@@ -226,6 +226,18 @@ int pbf_get_stream(pbf_ctx* ctx, void** stream);
 int pbf_sort_state(pbf_ctx* ctx, const float* pred,
                    uint32_t* keys, uint32_t* perm, uint32_t* cells);
 
+/* Sort state of the last substep, as the pipeline left it (the reference
+   keeps it in its sort and cell buffers after Step, src/Simulation.cpp:
+   466-536): the sorted keys and permutation (IntCeil(N, 2048) entries each,
+   the tail padded with 2147483646 and the identity as radixsort.cl:17 pads
+   it) and the cell table updateCells builds from those keys (2 *
+   gridBufSize words, x the scenes of a batch).  A parity hook: the keys and
+   permutation are copied from the sort's own buffers; the cell table, which
+   the substep resets after the friends build, is rebuilt from them by the
+   same kernel and reset again.  Any output may be NULL; the particle state
+   is not changed. */
+int pbf_read_sort(pbf_ctx* ctx, uint32_t* keys, uint32_t* perm, uint32_t* cells);
+
 /* Neighbour ("friends") list of the last substep, as used by the solver:
    counts[2*i+0] = entries used by computeScaling (circles kept while
    processed/total <= 0.6, compute_scaling.cl:47-54), counts[2*i+1] = entries
@@ -297,10 +309,15 @@ int pbf_use_graph(pbf_ctx* ctx, int enable);
    the GPU's memory budget).  It has no counterpart in the reference.
 
    Every pointer is a device address on the calling thread's current device:
-     d_pred  : float4 x params->particleCount predicted positions (input),
+     d_pred  : float4 x params->particleCount predicted positions (input,
+               16-byte aligned),
      d_keys  : params->particleCount sorted keys (output, no padding entries),
      d_perm  : params->particleCount sort permutation (output),
-     d_cells : 2 * params->gridBufSize words of cell table (output; may be NULL).
+     d_cells : 2 * params->gridBufSize words of cell table (output; may be NULL);
+   the last three 4-byte aligned.  A misaligned pointer, a host pointer, a
+   buffer or a stream of another device returns PBF_ERR_INVALID, and a CUDA
+   error left pending by earlier work returns PBF_ERR_CUDA (and stays
+   pending), all before any work is enqueued.
    The outputs equal the first particleCount keys / permutation entries and
    the cell table of pbf_sort_state.  Work is enqueued on `stream` (a
    cudaStream_t; NULL is the legacy default stream) and is complete when the

@@ -60,6 +60,10 @@ def lib() -> ctypes.CDLL:
         l.oracle_render.restype = c_int
         l.oracle_noise_sinf.argtypes = [c_float]
         l.oracle_noise_sinf.restype = c_float
+        l.oracle_load_scenario.argtypes = [ctypes.c_char_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]
+        l.oracle_load_scenario.restype = c_int
+        l.oracle_scene_block.argtypes = [c_int, c_int, c_int, c_float, c_void_p, c_float, ctypes.c_uint64, c_void_p]
+        l.oracle_scene_block.restype = c_int
         _lib = l
     return _lib
 
@@ -84,6 +88,9 @@ def ref() -> ctypes.CDLL:
         l.ref_set_force_mask.restype = None
         l.ref_set_threads.argtypes = [c_int]
         l.ref_set_threads.restype = None
+        l.ref_run_timed.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_double,
+                                    POINTER(c_int), POINTER(c_double)]
+        l.ref_run_timed.restype = c_int
         l.ref_max_threads.argtypes = []
         l.ref_max_threads.restype = c_int
         _ref = l
@@ -110,6 +117,37 @@ def ref_set_force_mask(mask=None):
     """The mask the shimmed reference computeDelta reads (its 14 planes are in its source)."""
     m = None if mask is None else np.ascontiguousarray(mask, np.uint32)
     ref().ref_set_force_mask(_ptr(m), 0 if m is None else m.shape[1], 0 if m is None else m.shape[0])
+
+
+def load_scenario(text: str, params_type):
+    """A scenario file's parameters and initial block, read the way the
+    reference's LoadParameters reads a `.par` file (oracle_load_scenario).
+    `params_type` is the ctypes mirror of PbfParameters to fill (zeroed
+    first).  Returns (params, (nx, ny, nz), origin, jitter, seed)."""
+    params = params_type()
+    dims = np.zeros(3, np.int32)
+    origin = np.zeros(3, np.float32)
+    jitter = c_float(0.0)
+    seed = ctypes.c_uint64(0)
+    lib().oracle_load_scenario(text.encode(), ctypes.byref(params), _ptr(dims), _ptr(origin), ctypes.byref(jitter),
+                               ctypes.byref(seed))
+    return params, tuple(int(d) for d in dims), origin, jitter.value, seed.value
+
+
+def make_scene(path, params_type):
+    """(params, pos[N,4], vel[N,4]) of a scenario file with an initial block
+    (BlockDims, BlockOrigin, Jitter, Seed): the same scene the product's
+    scenario reader builds, made here without the product library."""
+    from pathlib import Path
+    params, dims, origin, jitter, seed = load_scenario(Path(path).read_text(), params_type)
+    n = dims[0] * dims[1] * dims[2]
+    if n != params.particleCount:
+        raise ValueError(f"{path}: block holds {n} particles, ParticleCount is {params.particleCount}")
+    pos = np.zeros((n, 4), np.float32)
+    spacing = float(np.float32(params.h) * np.float32(params.setupSpacing))
+    if lib().oracle_scene_block(dims[0], dims[1], dims[2], spacing, _ptr(origin), jitter, seed, _ptr(pos)) != 0:
+        raise ValueError(f"{path}: no valid BlockDims")
+    return params, pos, np.zeros_like(pos)
 
 
 def set_wave_position(wave_pos: float = 0.0) -> None:
@@ -223,6 +261,23 @@ def ref_step(params, pos, vel, substeps=1, threads=0):
     if rc != 0:
         raise ValueError(f"ref_step_f32 rejected the input ({rc})")
     return pos, vel, pred, keys, perm, cells
+
+
+def ref_run_timed(params, pos, vel, warm, group, max_timed, budget_s, threads=0):
+    """The reference's kernels through the shim: `warm` untimed substeps, then
+    substeps timed in groups of `group` until `max_timed` have run or
+    `budget_s` seconds have passed (buffer setup outside the clock).
+    Returns (timed substeps, seconds, pos, vel)."""
+    ref().ref_set_threads(int(threads))
+    n = int(params.particleCount)
+    pos = np.array(pos, np.float32, copy=True).reshape(n, 4)
+    vel = np.array(vel, np.float32, copy=True).reshape(n, 4)
+    done, secs = c_int(0), c_double(0.0)
+    rc = ref().ref_run_timed(ctypes.byref(params), n, _ptr(pos), _ptr(vel), int(warm), int(group), int(max_timed),
+                             float(budget_s), ctypes.byref(done), ctypes.byref(secs))
+    if rc != 0:
+        raise ValueError(f"ref_run_timed rejected the input ({rc})")
+    return done.value, secs.value, pos, vel
 
 
 def ref_sort(params, pred):

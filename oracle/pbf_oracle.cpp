@@ -36,6 +36,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <random>
+#include <string>
 #include <vector>
 #include <omp.h>
 
@@ -1501,5 +1503,101 @@ int oracle_render(const PbfCamera* camp, int mode, int n, float h, const float* 
 
 // The force planes' noise sine, for the tests.
 float oracle_noise_sinf(float x) { return noise_sinf_ref(x); }
+
+// A scenario file read as the reference's LoadParameters reads it
+// (src/ParamUtils.cpp:24-100): '#' starts a comment, keys are
+// case-insensitive, each line's first word names a field and the next is
+// its value, the computed fields are set at the end (:97-99).  The keys the
+// benchmark's scenario files add are read too: the gravity vector, BoxClamp,
+// ZeroDistanceGuard, RelaxedMath, CompleteNeighbours, and the initial block
+// (BlockDims, BlockOrigin, Jitter, Seed).  `p` keeps the values of fields the
+// text does not name.  Returns the number of unknown keys.
+int oracle_load_scenario(const char* text, PbfParameters* p, int* dims, float* origin, float* jitter,
+                         uint64_t* seed) {
+    std::string all(text), line;
+    size_t at = 0;
+    int unknown = 0;
+    while (at < all.size()) {
+        const size_t nl = all.find('\n', at);
+        line = all.substr(at, nl == std::string::npos ? std::string::npos : nl - at);
+        at = nl == std::string::npos ? all.size() : nl + 1;
+        line.erase(std::find(line.begin(), line.end(), '#'), line.end());
+        for (char& ch : line) ch = (char)std::tolower((unsigned char)ch);
+        char key[64];
+        int used = 0;
+        if (std::sscanf(line.c_str(), " %63s%n", key, &used) != 1) continue;
+        const char* v = line.c_str() + used;
+        const std::string k(key);
+        auto F = [&](float& f) { std::sscanf(v, "%f", &f); };
+        auto U = [&](unsigned& u) { std::sscanf(v, "%u", &u); };
+        auto I = [&](int& i) { std::sscanf(v, "%d", &i); };
+        if (k == "resetsimonchange") I(p->resetSimOnChange);
+        else if (k == "particlecount") U(p->particleCount);
+        else if (k == "xmin") F(p->xMin);
+        else if (k == "xmax") F(p->xMax);
+        else if (k == "ymin") F(p->yMin);
+        else if (k == "ymax") F(p->yMax);
+        else if (k == "zmin") F(p->zMin);
+        else if (k == "zmax") F(p->zMax);
+        else if (k == "wavegenamp") F(p->waveGenAmp);
+        else if (k == "wavegenfreq") F(p->waveGenFreq);
+        else if (k == "wavegenduty") F(p->waveGenDuty);
+        else if (k == "timestep") F(p->timeStep);
+        else if (k == "simiterations") U(p->simIterations);
+        else if (k == "substeps") U(p->subSteps);
+        else if (k == "smoothlen") F(p->h);
+        else if (k == "gridbuffersize") U(p->gridBufSize);
+        else if (k == "restdensity") F(p->restDensity);
+        else if (k == "epsilon") F(p->epsilon);
+        else if (k == "garvity") F(p->garvity);
+        else if (k == "vorticityfactor") F(p->vorticityFactor);
+        else if (k == "viscosityfactor") F(p->viscosityFactor);
+        else if (k == "surfacetenstionk") F(p->surfaceTenstionK);
+        else if (k == "surfacetenstiondist") F(p->surfaceTenstionDist);
+        else if (k == "setupspacing") F(p->setupSpacing);
+        else if (k == "segmentsize") U(p->segmentSize);
+        else if (k == "sortiterations") U(p->sortIterations);
+        else if (k == "particlerendersize") F(p->particleRenderSize);
+        else if (k == "enablecachedbuffers") { int b = 0; I(b); p->EnableCachedBuffers = b != 0; }
+        else if (k == "gravityx") { F(p->gravityX); p->gravityVectorEnable = 1; }
+        else if (k == "gravityy") { F(p->gravityY); p->gravityVectorEnable = 1; }
+        else if (k == "gravityz") { F(p->gravityZ); p->gravityVectorEnable = 1; }
+        else if (k == "boxclamp") I(p->boxClamp);
+        else if (k == "zerodistanceguard") I(p->zeroDistanceGuard);
+        else if (k == "relaxedmath") I(p->relaxedMath);
+        else if (k == "completeneighbours") I(p->completeNeighbours);
+        else if (k == "blockdims") std::sscanf(v, "%d %d %d", &dims[0], &dims[1], &dims[2]);
+        else if (k == "blockorigin") std::sscanf(v, "%f %f %f", &origin[0], &origin[1], &origin[2]);
+        else if (k == "jitter") std::sscanf(v, "%f", jitter);
+        else if (k == "seed") { unsigned long long sd = 0; std::sscanf(v, "%llu", &sd); *seed = sd; }
+        else ++unknown;
+    }
+    p->h_2 = p->h * p->h;
+    p->friendsCircles = 5;
+    p->particlesPerCircle = 50;
+    return unknown;
+}
+
+// The benchmark scenes' initial block: nx x ny x nz particles at `spacing`
+// from the origin, x fastest, each coordinate moved by U(-jitter, jitter)
+// drawn from a 64-bit Mersenne Twister seeded with `seed` (53 bits of each
+// draw, in double, rounded once to float).
+int oracle_scene_block(int nx, int ny, int nz, float spacing, const float* origin, float jitter, uint64_t seed,
+                       float* pos) {
+    if (nx <= 0 || ny <= 0 || nz <= 0 || !pos) return -1;
+    std::mt19937_64 rng(seed);
+    size_t i = 0;
+    for (int iz = 0; iz < nz; ++iz)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int ix = 0; ix < nx; ++ix, ++i) {
+                const int idx[3] = {ix, iy, iz};
+                for (int c = 0; c < 3; ++c) {
+                    const double u = (double)(rng() >> 11) / 9007199254740992.0;
+                    pos[4 * i + c] = (float)((double)origin[c] + idx[c] * (double)spacing + (2.0 * u - 1.0) * (double)jitter);
+                }
+                pos[4 * i + 3] = 0.0f;
+            }
+    return 0;
+}
 
 }  // extern "C"

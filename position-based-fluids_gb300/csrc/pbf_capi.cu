@@ -1426,6 +1426,32 @@ int pbf_sort_state(pbf_ctx* ctx, const float* pred, uint32_t* keys, uint32_t* pe
     return PBF_OK;
 }
 
+int pbf_read_sort(pbf_ctx* ctx, uint32_t* keys, uint32_t* perm, uint32_t* cells) {
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    if (!ctx->stepped) return fail(ctx, PBF_ERR_STATE, "no substep has run yet");
+    PBF_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int n = ctx->n;
+    cudaStream_t s = ctx->stream;
+    const uint32_t* k = ctx->keys[ctx->keysIdx];
+    const uint32_t tableKeys = ctx->cellsWords * (uint32_t)(is_batch(ctx) ? ctx->sceneParams.size() : 1);
+    if (keys) PBF_CUDA(ctx, cudaMemcpyAsync(keys, k, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    if (perm) PBF_CUDA(ctx, cudaMemcpyAsync(perm, ctx->perm[ctx->keysIdx], 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    if (cells) {  // the substep's table, rebuilt in the (empty) table and cleared again
+        pbf::launch_update_cells(n, k, ctx->cells, tableKeys, ctx->errWord, s);
+        PBF_CUDA(ctx, cudaMemcpyAsync(cells, ctx->cells, 8 * (size_t)tableKeys, cudaMemcpyDeviceToHost, s));
+        pbf::launch_reset_cells(n, k, ctx->cells, tableKeys, ctx->errWord, s);
+    }
+    PBF_CUDA(ctx, cudaStreamSynchronize(s));
+    PBF_CUDA(ctx, cudaGetLastError());
+    const uint32_t nKeys = ((uint32_t)n + 2047u) / 2048u * 2048u;
+    for (uint32_t i = (uint32_t)n; i < nKeys; ++i) {
+        if (keys) keys[i] = 2147483646u;
+        if (perm) perm[i] = i;
+    }
+    return PBF_OK;
+}
+
 int pbf_read_friends(pbf_ctx* ctx, uint32_t* counts, uint32_t* list, int list_slots) {
     int rc = check_ready(ctx);
     if (rc) return rc;

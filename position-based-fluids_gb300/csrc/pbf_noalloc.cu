@@ -17,6 +17,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -62,6 +63,27 @@ int scratch_on_current_device(uint32_t** out) {
     return PBF_OK;
 }
 
+// PBF_OK when `ptr` is device (or managed) memory of device `dev`; a caller's
+// host pointer or a buffer of another GPU is refused here instead of faulting
+// the kernels.  `what` names the argument in the message.
+int check_device_pointer(const void* ptr, int dev, const char* what) {
+    cudaPointerAttributes a{};
+    const cudaError_t e = cudaPointerGetAttributes(&a, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // an unregistered address reports an error on some runtimes; it is this call's
+        return pbf::fail(nullptr, PBF_ERR_INVALID, std::string("pbf_sort_state_noalloc: ") + what +
+                                                       " is not a device address (" + cudaGetErrorString(e) + ")");
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+        return pbf::fail(nullptr, PBF_ERR_INVALID,
+                         std::string("pbf_sort_state_noalloc: ") + what + " is not device memory");
+    if (a.type == cudaMemoryTypeDevice && a.device != dev)
+        return pbf::fail(nullptr, PBF_ERR_INVALID, std::string("pbf_sort_state_noalloc: ") + what + " is on device " +
+                                                       std::to_string(a.device) + ", not the current device " +
+                                                       std::to_string(dev));
+    return PBF_OK;
+}
+
 }  // namespace
 
 extern "C" int pbf_sort_state_noalloc(const PbfParameters* params, const float* d_pred, uint32_t* d_keys,
@@ -76,9 +98,38 @@ extern "C" int pbf_sort_state_noalloc(const PbfParameters* params, const float* 
     if (params->gridBufSize < 1 || params->gridBufSize > (1u << 30))
         return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_sort_state_noalloc: gridBufSize must be in [1, 2^30]");
     if (!(params->h > 0.0f)) return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_sort_state_noalloc: SmoothLen must be positive");
+    // d_pred is read as float4 records, the others as 32-bit words
+    if (reinterpret_cast<uintptr_t>(d_pred) % 16 != 0)
+        return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_sort_state_noalloc: d_pred is not 16-byte aligned");
+    if (reinterpret_cast<uintptr_t>(d_keys) % 4 != 0 || reinterpret_cast<uintptr_t>(d_perm) % 4 != 0 ||
+        reinterpret_cast<uintptr_t>(d_cells) % 4 != 0)
+        return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_sort_state_noalloc: d_keys, d_perm and d_cells must be 4-byte aligned");
+    // An error left pending by the caller's earlier work would be read back
+    // below as this call's own; it is reported as the caller's and left set.
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess)
+        return pbf::fail(nullptr, PBF_ERR_CUDA, std::string("pbf_sort_state_noalloc: a CUDA error was pending before "
+                                                            "the call (nothing enqueued): ") + cudaGetErrorString(e));
     uint32_t* scratch = nullptr;
     int rc = scratch_on_current_device(&scratch);
     if (rc) return rc;
+    int dev = -1;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess)
+        return pbf::fail(nullptr, PBF_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if ((rc = check_device_pointer(d_pred, dev, "d_pred")) || (rc = check_device_pointer(d_keys, dev, "d_keys")) ||
+        (rc = check_device_pointer(d_perm, dev, "d_perm")) || (d_cells && (rc = check_device_pointer(d_cells, dev, "d_cells"))))
+        return rc;
+    if (stream) {  // a stream of another device would run the kernels there, against this device's scratch address
+        int sdev = -1;
+        if ((e = cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &sdev)) != cudaSuccess) {
+            cudaGetLastError();
+            return pbf::fail(nullptr, PBF_ERR_INVALID, std::string("pbf_sort_state_noalloc: stream: ") + cudaGetErrorString(e));
+        }
+        if (sdev != dev)
+            return pbf::fail(nullptr, PBF_ERR_INVALID, "pbf_sort_state_noalloc: stream belongs to device " +
+                                                           std::to_string(sdev) + ", not the current device " +
+                                                           std::to_string(dev));
+    }
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const pbf::DevConsts c = pbf::make_consts(*params, (int)n);
@@ -91,7 +142,6 @@ extern "C" int pbf_sort_state_noalloc(const PbfParameters* params, const float* 
 
     pbf::launch_compute_keys(c, pbf::Batch{nullptr, nullptr}, reinterpret_cast<const float4*>(d_pred), keys[0], perm[0], s);
     const int r = pbf::launch_radix_sort(plan, keys, perm, hist, nullptr, nullptr, nullptr, nullptr, s);
-    cudaError_t e = cudaSuccess;
     if (r == 1) {  // an odd number of passes left the result in the scratch half
         if ((e = cudaMemcpyAsync(d_keys, keys[1], 4 * (size_t)n, cudaMemcpyDeviceToDevice, s)) == cudaSuccess)
             e = cudaMemcpyAsync(d_perm, perm[1], 4 * (size_t)n, cudaMemcpyDeviceToDevice, s);

@@ -134,6 +134,7 @@ def library() -> ctypes.CDLL:
         "pbf_get_stream": [c_void_p, POINTER(c_void_p)],
         "pbf_sort_state": [c_void_p, f32p, u32p, u32p, u32p],
         "pbf_read_friends": [c_void_p, u32p, u32p, c_int],
+        "pbf_read_sort": [c_void_p, u32p, u32p, u32p],
         "pbf_enable_stage_timing": [c_void_p, c_int],
         "pbf_stage_timings": [c_void_p, f32p, c_int, POINTER(c_int), c_char_p, c_size_t],
         "pbf_launch_count": [c_void_p, POINTER(c_uint64)],
@@ -377,6 +378,17 @@ class Simulation:
         _check(self.lib.pbf_sort_state(self._ctx, _f32(pred), _u32(keys), _u32(perm), _u32(cells)), self._ctx)
         return keys, perm, cells
 
+    def read_sort(self):
+        """Keys and permutation (IntCeil(N, 2048) entries) and the cell table
+        of the last substep, as the pipeline computed them."""
+        nkeys = (self.n + 2047) // 2048 * 2048
+        keys = np.empty(nkeys, np.uint32)
+        perm = np.empty(nkeys, np.uint32)
+        scenes = len(self.scene_params) if self.scene_params else 1
+        cells = np.empty(2 * self.params.gridBufSize * scenes, np.uint32)
+        _check(self.lib.pbf_read_sort(self._ctx, _u32(keys), _u32(perm), _u32(cells)), self._ctx)
+        return keys, perm, cells
+
     def read_friends(self, slots: int | None = None):
         """(counts[N,2], list[slots,N]) of the last substep."""
         if slots is None:
@@ -508,7 +520,7 @@ EXPORTED_SYMBOLS = sorted(
         "pbf_default_parameters", "pbf_load_parameters", "pbf_create", "pbf_destroy", "pbf_init_buffers",
         "pbf_init_cells", "pbf_load_force_masks", "pbf_init_kernels", "pbf_set_params", "pbf_set_pause",
         "pbf_step", "pbf_step_async", "pbf_synchronize", "pbf_read_state", "pbf_write_state",
-        "pbf_device_positions", "pbf_get_stream", "pbf_sort_state", "pbf_read_friends",
+        "pbf_device_positions", "pbf_get_stream", "pbf_sort_state", "pbf_read_sort", "pbf_read_friends",
         "pbf_enable_stage_timing", "pbf_stage_timings", "pbf_launch_count", "pbf_use_graph",
         "pbf_reference_lattice", "pbf_scene_block", "pbf_sort_state_noalloc", "pbf_scene_double_dam_break",
         "pbf_create_batch", "pbf_scene_offsets", "pbf_get_launch_shape", "pbf_set_launch_shape", "pbf_autotune",

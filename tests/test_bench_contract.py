@@ -50,4 +50,53 @@ def test_reference_arm_prints_the_contract_line():
         assert key in line, key
     assert line["cpu_baseline"]["kind"] in ("reference", "port") and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
-    assert line["warmup"] == 3 and 1 <= line["steps"] <= 2  # untimed warm-up substeps, then the timed ones
+    assert line["warmup"] == 3 and 1 <= line["steps"] <= 2  # untimed warm-up frames, then the timed ones
+    for key in ("epsilon 20000", "s_corr k 0.001", "XSPH c"):
+        assert key in line["config"]["workload"], key
+
+
+def test_reference_scene_leaves_the_product_library_unloaded():
+    """The reference arm builds its scene through the oracle: the same
+    parameters and positions as the product's scenario reader, with
+    libpbf_gb300.so never mapped into the process."""
+    import subprocess
+    code = (
+        "import sys; sys.path[:0] = [%r, %r]\n"
+        "import bench\n"
+        "params, pos, vel = bench.reference_scene('dam_break_32k')\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert 'libpbf_gb300' not in maps, 'product library mapped'\n"
+        "assert 'libpbf_oracle' in maps\n"
+        "import numpy as np, pbf\n"
+        "p2, pos2, _ = pbf.make_scene('dam_break_32k')\n"
+        "assert bytes(params) == bytes(p2) and np.array_equal(pos.view(np.uint32), pos2.view(np.uint32))\n"
+        "print('ok')\n" % (str(REPO), str(REPO / "position-based-fluids_gb300")))
+    run = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0 and run.stdout.strip() == "ok", run.stderr[-2000:]
+
+
+def test_survey_byte_model_sums_to_the_substep_total():
+    """The per-stage byte model adds up to 444 + 56 I bytes per particle and
+    substep (3 sort passes)."""
+    import bench
+    it = 4
+    per_substep = ["predictPositions", "radixsort", "sortParticles", "updateCells", "updateVelocities",
+                   "applyViscosity", "applyVorticity"]
+    total = sum(bench.survey_bytes(k) for k in per_substep) + it * (bench.survey_bytes("computeScaling") +
+                                                                   bench.survey_bytes("computeDelta"))
+    assert total == 444.0 + 56.0 * it
+    assert bench.survey_bytes("buildFriendsList") is None
+
+
+def test_stage_rooflines_and_dominant_kernel():
+    import bench
+    stage_ms = {"computeScaling": 1.0, "computeDelta": 0.8, "buildFriendsList": 0.9, "radixsort": 0.1}
+    n, it, sub = 1 << 20, 4, 2
+    rows = bench.stage_rooflines(stage_ms, n, it, sub, 30.0, 26.0, 6700.0)
+    assert rows["computeScaling"]["launches_per_step"] == 8 and rows["radixsort"]["launches_per_step"] == 2
+    assert rows["computeScaling"]["bytes_per_launch"] == 20.0 * n
+    assert "frac" not in rows["buildFriendsList"] and rows["buildFriendsList"]["frac_with_lists"] > 0
+    roof = bench.dominant_roofline(stage_ms, n, it, sub, 30.0, 26.0, 6700.0, "measured")
+    assert roof["kernel"] == "computeScaling"
+    assert abs(roof["achieved"] - 20.0 * n / (1.0 / 8 / 1e3) / 1e9) < 1e-6
+    assert roof["frac_with_lists"] > roof["frac"]

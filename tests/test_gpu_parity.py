@@ -52,7 +52,9 @@ def assert_same(name, got, want):
         raise AssertionError(f"{name}: {nbad} words differ (rel err {rel:.3e}, NaN mismatches {nan_mismatch})")
 
 
-def run_gpu(pbf, params, pos, vel, substeps, device, graph=True, friends=True, algorithm=None):
+def run_gpu(pbf, params, pos, vel, substeps, device, graph=True, friends=True, algorithm=None, sort=None):
+    """`sort` (a dict, optional) receives the keys, permutation and cell table
+    of the last substep (pbf_read_sort)."""
     with pbf.Simulation.create(params, pos, vel, device=device) as sim:
         sim.use_graph(graph)
         if algorithm is not None:  # friends algorithm; the balanced map with the warp one
@@ -60,6 +62,8 @@ def run_gpu(pbf, params, pos, vel, substeps, device, graph=True, friends=True, a
         sim.Step(substeps)
         p, v, pr = sim.read_state()
         counts, lst = sim.read_friends() if friends else (None, None)
+        if sort is not None:
+            sort["keys"], sort["perm"], sort["cells"] = sim.read_sort()
     return p, v, pr, counts, lst
 
 
@@ -119,11 +123,17 @@ MANIFEST = json.loads((GOLDEN / "golden.json").read_text())
 @pytest.mark.parametrize("algorithm", [0, 1, 2], ids=["scan", "warp", "brick"])
 @pytest.mark.parametrize("case", MANIFEST["cases"], ids=[c["name"] for c in MANIFEST["cases"]])
 def test_gpu_matches_reference_kernel_digests(case, algorithm, pbf_mod, cuda_device):
-    """Outputs of the reference's own kernels (tests/golden) reproduced on the GPU."""
+    """Outputs of the reference's own kernels (tests/golden) reproduced on the
+    GPU: positions, velocities and predictions after the last substep, and
+    that substep's sorted keys, permutation and cell table (the reference's
+    histogram / scan / paste / reorder and updateCells, radixsort.cl:61-308,
+    update_cells.cl) as the GPU pipeline computed them."""
     params, pos, vel = mg().scene(tuple(case["block"]), case["overrides"])
+    sort = {}
     p, v, pr, _, _ = run_gpu(pbf_mod, params, pos, vel, case["substeps"], cuda_device, friends=False,
-                             algorithm=algorithm)
-    for name, arr in (("pos", p), ("vel", v), ("pred", pr)):
+                             algorithm=algorithm, sort=sort)
+    for name, arr in (("pos", p), ("vel", v), ("pred", pr), ("keys", sort["keys"]), ("perm", sort["perm"]),
+                      ("cells", sort["cells"])):
         assert mg().digest(arr) == case["sha256"][name], f"{case['name']}: {name}"
 
 

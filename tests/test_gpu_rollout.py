@@ -111,7 +111,17 @@ def test_graph_and_eager_reverse_passes_agree(pbf_mod, case, cuda_device):
 
 def test_adjoint_matches_central_differences(pbf_mod, case, cuda_device):
     """Directional derivatives of the GPU gradient against central
-    differences (step 1e-3) of the FP64 replay on 64 random directions."""
+    differences (step 1e-3) of the FP64 replay on 64 random unit directions.
+
+    Two bounds, both GRAD_TOL: the median relative error |fd - ad| / |ad|,
+    and the maximum over all 64 directions of |fd - ad| / |grad L|.  The
+    second is the per-direction bound: a unit direction's derivative is at
+    most |grad L|, and the relative error of one direction is unbounded where
+    that direction is nearly orthogonal to the gradient (|ad| -> 0), since
+    the FP32 gradient's own error (about 3e-4 of its norm) does not shrink
+    with ad.  The FP32 reverse pass of the oracle gives a median of 2.3e-4,
+    a scaled maximum of 5.7e-6 and a largest plain relative error of 4.5e-2
+    on these 64 directions."""
     params, pos, vel, R, target = case
     n = R.n
     with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
@@ -121,7 +131,9 @@ def test_adjoint_matches_central_differences(pbf_mod, case, cuda_device):
     c0 = float(params.viscosityFactor)
     v0 = R.vel0.astype(np.float64)
     rng = np.random.default_rng(5)
-    rel = []
+    rel, scaled = [], []
+    gnorm = float(np.sqrt((dv[:, :3].astype(np.float64) ** 2).sum() + (float(dc) * 1e-6) ** 2 +
+                          (np.asarray(dg, np.float64) ** 2).sum()))
     for _ in range(64):
         d = rng.normal(0.0, 1.0, 3 * n + 4)
         d /= np.linalg.norm(d)
@@ -132,9 +144,12 @@ def test_adjoint_matches_central_differences(pbf_mod, case, cuda_device):
         fd = (L(1e-3) - L(-1e-3)) / 2e-3
         ad = float((dv.astype(np.float64) * d_v).sum() + dc * d_c + (dg.astype(np.float64) * d_g).sum())
         rel.append(abs(fd - ad) / max(abs(ad), 1e-30))
-    rel = np.array(rel)
-    print(f"GPU adjoint vs central differences: median {np.median(rel):.2e}, max {rel.max():.2e}")
+        scaled.append(abs(fd - ad) / gnorm)
+    rel, scaled = np.array(rel), np.array(scaled)
+    print(f"GPU adjoint vs central differences: median {np.median(rel):.2e}, max {rel.max():.2e}; "
+          f"|fd - ad| / |grad L|: max {scaled.max():.2e}")
     assert np.median(rel) < GRAD_TOL
+    assert scaled.max() < GRAD_TOL
 
 
 def test_torch_autograd_wrapper(pbf_mod, case, cuda_device):
