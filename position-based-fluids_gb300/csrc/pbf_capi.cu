@@ -226,6 +226,23 @@ DevConsts make_consts(const PbfParameters& p, int n) {
     c.complete = p.completeNeighbours ? 1 : 0;
     c.dpScale = c.negGradSpiky / c.rho0;
     c.invPoly6q = 1.0f / c.poly6q;
+    // Exact-mode quotients by reciprocal (quotient_rn in pbf_device.cuh).  With
+    // every coordinate 0 or at least 2^-37 in magnitude, a coordinate
+    // difference is 0 or at least 2^-60, and |r| (when r != 0) is normal.  A
+    // nonzero remaining distance h - |r| is at least h 2^-25 (one half ulp of
+    // h), so the density pass's numerator gradSpiky (h - |r|)^2 r_x is 0 or at
+    // least gradSpiky (h 2^-25)^2 2^-60, which must not fall below 2^-100; the
+    // quotients themselves are at most gradSpiky h^2 (|r_x| <= |r|).
+    const double hrMin = (double)p.h * std::ldexp(1.0, -25);
+    c.quotients = (p.h >= std::ldexp(1.0f, -10) && p.h <= 1024.0f &&
+                   (double)c.gradSpiky * hrMin * hrMin >= std::ldexp(1.0, -40) &&
+                   (double)c.gradSpiky * (double)p.h * (double)p.h < 1e30) ? 1 : 0;
+    // s_corr: for r^2 < h^2 the numerator (h^2 - r^2)^3 is at least
+    // (h^2 2^-25)^3 >= 2^-99 when h^2 >= 2^-8, and with poly6q <= h^6 <= 1 the
+    // quotient is at least as large; at most h^6 / poly6q.
+    c.recipPoly6q = 1.0f / c.poly6q;
+    c.quotientPoly6q = (std::isnormal(c.poly6q) && std::isnormal(c.recipPoly6q) && c.h2 >= std::ldexp(1.0f, -8) &&
+                        c.h2 <= 1.0f && (double)c.h2 * c.h2 * c.h2 / c.poly6q < 1e30) ? 1 : 0;
     c.circles = (int)p.friendsCircles;
     c.perCircle = (int)p.particlesPerCircle;
     c.grid = p.gridBufSize;
@@ -307,6 +324,7 @@ void apply_planes(pbf_ctx* ctx) {
     ctx->consts.maskH = ctx->maskH;
     ctx->consts.wave = ctx->waveDev;
     ctx->consts.err = ctx->errWord;
+    ctx->consts.irregular = ctx->errWord + 1;
 }
 
 // The captured substep; the reverse pass's segment graphs are dropped with
@@ -830,8 +848,9 @@ int pbf_create(const PbfParameters* params, int device, pbf_ctx** out) {
     ctx->device = device;
     PBF_CUDA(nullptr, cudaSetDevice(device));
     PBF_CUDA(nullptr, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-    PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->errWord, sizeof(int)));
-    PBF_CUDA(nullptr, cudaMemset(ctx->errWord, 0, sizeof(int)));
+    // [0]: the error word; [1]: the sticky "irregular coordinate" flag of the exact quotients
+    PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->errWord, 2 * sizeof(int)));
+    PBF_CUDA(nullptr, cudaMemset(ctx->errWord, 0, 2 * sizeof(int)));
     *out = ctx.release();
     return PBF_OK;
 }
@@ -1342,6 +1361,8 @@ int pbf_write_state_async(pbf_ctx* ctx, const float* pos, const float* vel) {
     const size_t bytes = 16 * (size_t)ctx->n;
     if (pos) {
         PBF_CUDA(ctx, cudaMemcpyAsync(ctx->pos[ctx->curPos], pos, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        // new positions: the irregular-coordinate flag starts over (predict checks every prediction)
+        PBF_CUDA(ctx, cudaMemsetAsync(ctx->errWord + 1, 0, sizeof(int), ctx->stream));
         // the written records become particles 0 .. N-1
         iota_kernel<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->ids);
         PBF_CUDA(ctx, cudaGetLastError());

@@ -44,6 +44,15 @@ struct DevConsts {
     const float* wave;           // device scalar: the moving wall's offset from xMin (NULL: none)
     int* err;                    // the context's error word (bounds-checked builds record bad indices there)
     float dpScale, invPoly6q;    // -gradSpiky / rho0 and 1 / poly6q (relaxed variants only)
+    // Exact passes: quotients by |r| and by poly6q through a correctly rounded
+    // reciprocal and one remainder correction (quotient_rn), where the
+    // parameters keep every numerator and quotient in the range that makes it
+    // equal to IEEE division (make_consts decides), and while no predicted
+    // coordinate is tiny and nonzero (*irregular stays 0; see note_irregular).
+    int quotients;               // divisions by |r| in the four neighbour passes
+    int quotientPoly6q;          // the s_corr division by poly6q in the position pass
+    float recipPoly6q;           // RN(1 / poly6q)
+    int* irregular;              // device word, sticky: a predicted coordinate in (0, 2^-37) was written
     int circles, perCircle;
     uint32_t grid;
     int n;

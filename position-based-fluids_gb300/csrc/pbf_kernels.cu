@@ -71,6 +71,7 @@ __global__ void predict_keys_kernel(DevConsts c, Batch b, const float4* __restri
     const float4 p = pos[i];
     const float4 q = make_float4(p.x + c.dt * v.x, p.y + c.dt * v.y, p.z + c.dt * v.z, p.w + c.dt * v.w);
     pred[i] = q;
+    note_irregular(c.irregular, q.x, q.y, q.z);
     if (!paused) {
         keys[i] = base + grid_hash(__float2int_rz(q.x / c.h), __float2int_rz(q.y / c.h), __float2int_rz(q.z / c.h), c.grid);
         perm[i] = (uint32_t)i;
@@ -576,13 +577,13 @@ __device__ __forceinline__ float spiky_over_r(const DevConsts& c, float r2, floa
     return hr * hr * w;
 }
 
-// compute_scaling.cl:27-112 followed by pack_data.cl (w = lambda).
-template <bool R, bool B, int W>
-__global__ void __launch_bounds__(kMaxBlock)
-compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __restrict__ predPacked,
-                       float* __restrict__ density, const uint32_t* __restrict__ list,
-                       const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn,
-                       uint32_t* __restrict__ flatOut) {
+// compute_scaling.cl:27-112 followed by pack_data.cl (w = lambda).  Q: the
+// exact quotients by |r| through one reciprocal (quotient_rn).
+template <bool R, bool B, int W, bool Q>
+__device__ __forceinline__ void compute_scaling_body(const DevConsts& c, const float4* __restrict__ pred,
+                                                     float4* __restrict__ predPacked, float* __restrict__ density,
+                                                     const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
+                                                     const uint32_t* __restrict__ flatIn, uint32_t* __restrict__ flatOut) {
     const int n = c.n;
     const int i = B ? balanced_particle(meta, n, true) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i < 0 || i >= n) return;
@@ -613,7 +614,17 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
                 const float rl = sqrtf(r2);
                 const float hr = c.h - rl;
                 const float sc = c.gradSpiky * hr * hr;
-                const float g0 = (sc * rx) / rl, g1 = (sc * ry) / rl, g2 = (sc * rz) / rl;
+                float g0, g1, g2;
+                if (Q) {
+                    const float y = __frcp_rn(rl);
+                    g0 = quotient_rn(sc * rx, rl, y);
+                    g1 = quotient_rn(sc * ry, rl, y);
+                    g2 = quotient_rn(sc * rz, rl, y);
+                } else {
+                    g0 = (sc * rx) / rl;
+                    g1 = (sc * ry) / rl;
+                    g2 = (sc * rz) / rl;
+                }
                 const float d = c.h2 - r2;
                 ds = ds + d * d * d;
                 gsk = gsk + dot3(g0, g1, g2, g0, g1, g2);
@@ -631,17 +642,27 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
     predPacked[i] = make_float4(pi.x, pi.y, pi.z, lambda);
 }
 
+template <bool R, bool B, int W>
+__global__ void __launch_bounds__(kMaxBlock)
+compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __restrict__ predPacked,
+                       float* __restrict__ density, const uint32_t* __restrict__ list,
+                       const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn,
+                       uint32_t* __restrict__ flatOut) {
+    if (!R && exact_quotients(c)) compute_scaling_body<R, B, W, true>(c, pred, predPacked, density, list, meta, flatIn, flatOut);
+    else compute_scaling_body<R, B, W, false>(c, pred, predPacked, density, list, meta, flatIn, flatOut);
+}
+
 // ---------------------------------------------------------------- delta --
 // compute_delta.cl:54-185 (force planes: identity for an all-zero mask) with
 // the optional box clamp on `future`, then update_predicted.cl.  After the
 // last iteration w carries the density (pack_data.cl with the density source,
 // src/Simulation.cpp:591).
-template <bool R, bool B, int W>
-__global__ void __launch_bounds__(kMaxBlock)
-compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const float4* __restrict__ posPrev,
-                     float4* __restrict__ predOut, const float* __restrict__ density, const uint32_t* __restrict__ list,
-                     const uint2* __restrict__ meta, int lastIteration, uint8_t* __restrict__ clampMask,
-                     const uint32_t* __restrict__ flatIn) {
+template <bool R, bool B, int W, bool Q>
+__device__ __forceinline__ void compute_delta_body(const DevConsts& c, const Batch& b, const float4* __restrict__ pp,
+                                                   const float4* __restrict__ posPrev, float4* __restrict__ predOut,
+                                                   const float* __restrict__ density, const uint32_t* __restrict__ list,
+                                                   const uint2* __restrict__ meta, int lastIteration,
+                                                   uint8_t* __restrict__ clampMask, const uint32_t* __restrict__ flatIn) {
     const int n = c.n;
     const int i = B ? balanced_particle(meta, n, false) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i < 0 || i >= n) return;
@@ -670,10 +691,20 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const 
             if (in_support(c, r2)) {
                 const float rl = sqrtf(r2);
                 const float hr = c.h - rl;
-                const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
+                float g0, g1, g2;
+                if (Q) {
+                    const float y = __frcp_rn(rl);
+                    g0 = quotient_rn(rx, rl, y) * hr * hr;
+                    g1 = quotient_rn(ry, rl, y) * hr * hr;
+                    g2 = quotient_rn(rz, rl, y) * hr * hr;
+                } else {
+                    g0 = (rx / rl) * hr * hr;
+                    g1 = (ry / rl) * hr * hr;
+                    g2 = (rz / rl) * hr * hr;
+                }
                 const float d = c.h2 - r2;
                 const float p6 = d * d * d;
-                const float rq = p6 / c.poly6q;
+                const float rq = c.quotientPoly6q ? quotient_rn(p6, c.poly6q, c.recipPoly6q) : p6 / c.poly6q;
                 const float scorr = c.K * rq * rq * rq * rq;
                 const float a = pi.w + pj.w + scorr;
                 sx = sx + a * g0;
@@ -717,7 +748,21 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const 
         clampMask[i] = 0;
     }
     const float dx = fx - pi.x, dy = fy - pi.y, dz = fz - pi.z;
-    predOut[i] = make_float4(pi.x + dx, pi.y + dy, pi.z + dz, lastIteration ? density[i] : pi.w + 0.0f);
+    const float4 out = make_float4(pi.x + dx, pi.y + dy, pi.z + dz, lastIteration ? density[i] : pi.w + 0.0f);
+    predOut[i] = out;
+    note_irregular(c.irregular, out.x, out.y, out.z);
+}
+
+template <bool R, bool B, int W>
+__global__ void __launch_bounds__(kMaxBlock)
+compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const float4* __restrict__ posPrev,
+                     float4* __restrict__ predOut, const float* __restrict__ density, const uint32_t* __restrict__ list,
+                     const uint2* __restrict__ meta, int lastIteration, uint8_t* __restrict__ clampMask,
+                     const uint32_t* __restrict__ flatIn) {
+    if (!R && exact_quotients(c))
+        compute_delta_body<R, B, W, true>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn);
+    else
+        compute_delta_body<R, B, W, false>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn);
 }
 
 // ----------------------------------------------------------- velocities --
@@ -740,13 +785,14 @@ __global__ void update_velocities_kernel(DevConsts c, const float4* __restrict__
 }
 
 // apply_viscosity.cl:12-86, every neighbour read from the pre-pass
-// velocities (Jacobi).
-template <bool R, bool B, int W>
-__global__ void __launch_bounds__(kMaxBlock)
-apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const float4* __restrict__ velIn,
-                       float4* __restrict__ velOut, float4* __restrict__ omega,
-                       const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
-                       const uint32_t* __restrict__ flatIn) {
+// velocities (Jacobi).  omega.w receives |omega| (sqrt of its dot product, as
+// apply_vorticity.cl:55 forms it for each neighbour), so that the vorticity
+// pass reads it instead of recomputing it per pair.
+template <bool R, bool B, int W, bool Q>
+__device__ __forceinline__ void apply_viscosity_body(const DevConsts& c, const Batch& b, const float4* __restrict__ pred,
+                                                     const float4* __restrict__ velIn, float4* __restrict__ velOut,
+                                                     float4* __restrict__ omega, const uint32_t* __restrict__ list,
+                                                     const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn) {
     const int n = c.n;
     const int i = B ? balanced_particle(meta, n, false) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i < 0 || i >= n) return;
@@ -777,7 +823,17 @@ apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, co
             } else {
                 const float rl = sqrtf(r2);
                 const float hr = c.h - rl;
-                const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
+                float g0, g1, g2;
+                if (Q) {
+                    const float y = __frcp_rn(rl);
+                    g0 = quotient_rn(rx, rl, y) * hr * hr;
+                    g1 = quotient_rn(ry, rl, y) * hr * hr;
+                    g2 = quotient_rn(rz, rl, y) * hr * hr;
+                } else {
+                    g0 = (rx / rl) * hr * hr;
+                    g1 = (ry / rl) * hr * hr;
+                    g2 = (rz / rl) * hr * hr;
+                }
                 ox = ox + (uy * g2 - uz * g1);
                 oy = oy + (uz * g0 - ux * g2);
                 oz = oz + (ux * g1 - uy * g0);
@@ -793,16 +849,26 @@ apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, co
     vsz = vsz * c.poly6;
     const float visc = b.scenes ? b.scenes[b.sceneOf[i]].visc : c.visc;
     velOut[i] = make_float4(vi.x + visc * vsx, vi.y + visc * vsy, vi.z + visc * vsz, vi.w + visc * 0.0f);
-    omega[i] = make_float4(ox * c.negGradSpiky, oy * c.negGradSpiky, oz * c.negGradSpiky, 0.0f);
+    const float wx = ox * c.negGradSpiky, wy = oy * c.negGradSpiky, wz = oz * c.negGradSpiky;
+    omega[i] = make_float4(wx, wy, wz, sqrtf(dot3(wx, wy, wz, wx, wy, wz)));
 }
 
-// apply_vorticity.cl:12-86
 template <bool R, bool B, int W>
 __global__ void __launch_bounds__(kMaxBlock)
-apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
-                       const float4* __restrict__ velIn, float4* __restrict__ velOut,
+apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const float4* __restrict__ velIn,
+                       float4* __restrict__ velOut, float4* __restrict__ omega,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
                        const uint32_t* __restrict__ flatIn) {
+    if (!R && exact_quotients(c)) apply_viscosity_body<R, B, W, true>(c, b, pred, velIn, velOut, omega, list, meta, flatIn);
+    else apply_viscosity_body<R, B, W, false>(c, b, pred, velIn, velOut, omega, list, meta, flatIn);
+}
+
+// apply_vorticity.cl:12-86; |omega_j| is read from omega.w (apply_viscosity).
+template <bool R, bool B, int W, bool Q>
+__device__ __forceinline__ void apply_vorticity_body(const DevConsts& c, const float4* __restrict__ pred,
+                                                     const float4* __restrict__ omega, const float4* __restrict__ velIn,
+                                                     float4* __restrict__ velOut, const uint32_t* __restrict__ list,
+                                                     const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn) {
     const int n = c.n;
     const int i = B ? balanced_particle(meta, n, false) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (i < 0 || i >= n) return;
@@ -828,8 +894,18 @@ apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float
             } else {
                 const float rl = sqrtf(r2);
                 const float hr = c.h - rl;
-                const float g0 = (rx / rl) * hr * hr, g1 = (ry / rl) * hr * hr, g2 = (rz / rl) * hr * hr;
-                const float ol = sqrtf(dot3(oj.x, oj.y, oj.z, oj.x, oj.y, oj.z));
+                float g0, g1, g2;
+                if (Q) {
+                    const float y = __frcp_rn(rl);
+                    g0 = quotient_rn(rx, rl, y) * hr * hr;
+                    g1 = quotient_rn(ry, rl, y) * hr * hr;
+                    g2 = quotient_rn(rz, rl, y) * hr * hr;
+                } else {
+                    g0 = (rx / rl) * hr * hr;
+                    g1 = (ry / rl) * hr * hr;
+                    g2 = (rz / rl) * hr * hr;
+                }
+                const float ol = oj.w;  // sqrt(dot(omega_j, omega_j)), formed once by apply_viscosity
                 ex = ex + ol * g0;
                 ey = ey + ol * g1;
                 ez = ez + ol * g2;
@@ -861,6 +937,16 @@ apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float
     const float fz = c.vort * (ex * oi.y - ey * oi.x);
     const float4 v = velIn[i];
     velOut[i] = make_float4(v.x + fx * c.dt, v.y + fy * c.dt, v.z + fz * c.dt, v.w + 0.0f);
+}
+
+template <bool R, bool B, int W>
+__global__ void __launch_bounds__(kMaxBlock)
+apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
+                       const float4* __restrict__ velIn, float4* __restrict__ velOut,
+                       const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
+                       const uint32_t* __restrict__ flatIn) {
+    if (!R && exact_quotients(c)) apply_vorticity_body<R, B, W, true>(c, pred, omega, velIn, velOut, list, meta, flatIn);
+    else apply_vorticity_body<R, B, W, false>(c, pred, omega, velIn, velOut, list, meta, flatIn);
 }
 
 }  // namespace

@@ -155,6 +155,9 @@ SUBSTEP_CASES = {
     # bits come from negative integers) and past 1024 cells along x (the
     # 10-bit Morton coordinates wrap, so distant cells share hashes)
     "across_origin": (dict(dims=(12, 12, 12), origin=(-0.3,) * 3, boxClamp=0), 3),
+    # no jitter: many neighbours share a coordinate, so the numerators of the
+    # exact passes' quotients by |r| are exactly zero
+    "lattice_without_jitter": (dict(dims=(14, 14, 14), jitter=0.0), 3),
     "beyond_morton_range": (dict(dims=(8, 8, 8), origin=(102.2, 0.025, 0.025), boxClamp=0), 3),
 }
 
@@ -175,6 +178,25 @@ def test_substeps_bit_exact(name, algorithm, pbf_mod, oracle_mod, cuda_device):
     for s in range(slots):
         used = dbg["counts"][:, 0] > s
         assert np.array_equal(glist[s][used], dbg["list"][s][used]), f"friend list slot {s}"
+    assert_same("pos", gp, op)
+    assert_same("vel", gv, ov)
+    assert_same("pred", gpr, opr)
+
+
+def test_tiny_coordinates_bit_exact(pbf_mod, oracle_mod, cuda_device):
+    """Predicted coordinates in (0, 2^-37): their differences can be too small
+    for the exact passes' quotients through one reciprocal, so the library
+    notices them as predict writes them and divides the IEEE way from then
+    on.  A block at the origin (no clamp) with some particles moved onto tiny
+    coordinates next to neighbours at exactly 0."""
+    params, pos, vel = scene(pbf_mod, (10, 10, 10), origin=(0.0, 0.0, 0.0), jitter=0.0, boxClamp=0)
+    pos[1, 0] = np.float32(3e-13)       # x next to particle 0 at x = 0
+    pos[10, 1] = np.float32(1e-30)      # y, a normal float far below 2^-37
+    pos[100, 2] = np.float32(2e-42)     # z, subnormal
+    pos[111, :3] = np.float32(5e-39)
+    gp, gv, gpr, gcounts, glist = run_gpu(pbf_mod, params, pos, vel, 3, cuda_device)
+    op, ov, opr, dbg = oracle_mod.step(params, pos, vel, 3, debug=True)
+    assert np.array_equal(gcounts, dbg["counts"]), "friend counts"
     assert_same("pos", gp, op)
     assert_same("vel", gv, ov)
     assert_same("pred", gpr, opr)
