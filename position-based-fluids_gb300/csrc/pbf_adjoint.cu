@@ -11,7 +11,8 @@
 //   v2 = (p^I - x)/dt,  v3 = v2 + c POLY6 sum (v2_j - v2_i) W,
 //   omega_i = -G sum (v2_j - v2_i) x k,  eta_i = -G sum |omega_j| k,
 //   v4 = v3 + dt eps_v (eta/|eta|) x omega_i.
-// Each kernel below walks the same friend rows as its forward kernel and
+// Each kernel below walks the same friends as its forward kernel (the flat
+// rows the substep recorded: friend t of particle i at list[t * N + i]) and
 // scatters neighbour terms with atomics, so the sums are not ordered: these
 // are FP32 gradients, not bit-reproducible ones.  The derivation is the same
 // as the FP64 adjoint the tests compare against.
@@ -79,9 +80,9 @@ adj_vorticity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
     const F3 pi = f3(pI[i]);
     const float G = c.gradSpiky;
     F3 eta = {0.0f, 0.0f, 0.0f};
-    FriendRows f1(mt, kept_other(mt), c.perCircle);
+    FlatFriends f1(mt, kept_other(mt));
     for (int t = 0; t < f1.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)f1.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
+        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const float4 pj = pI[j];
         const F3 r = pi - f3(pj);
         const float r2 = dot(r, r);
@@ -97,9 +98,9 @@ adj_vorticity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
     const F3 Nb = cross(oi, ub);
     add3(&omb[i], cross(ub, N));
     const F3 etab = (1.0f / l) * (Nb - dot(N, Nb) * N);
-    FriendRows f2(mt, kept_other(mt), c.perCircle);
+    FlatFriends f2(mt, kept_other(mt));
     for (int t = 0; t < f2.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)f2.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
+        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const float4 pj = pI[j];
         const F3 r = pi - f3(pj);
         const float r2 = dot(r, r);
@@ -130,9 +131,9 @@ adj_viscosity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
         const F3 pi = f3(pI[i]), v3b = f3(vb[i]), ob = f3(omb[i]), vi = f3(v2[i]);
         const float G = c.gradSpiky;
         add3(&v2b[i], v3b);
-        FriendRows fr(mt, kept_other(mt), c.perCircle);
+        FlatFriends fr(mt, kept_other(mt));
         for (int t = 0; t < fr.total; ++t) {
-            const uint32_t j = checked_index(list[(size_t)fr.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
+            const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
             const float4 pj = pI[j];
             const F3 r = pi - f3(pj);
             const float r2 = dot(r, r);
@@ -188,9 +189,9 @@ adj_delta_kernel(DevConsts c, const float4* __restrict__ q, const uint8_t* __res
     const F3 pi = f3(qi);
     const float a0 = -c.gradSpiky / c.rho0;
     const uint64_t mt = load_meta(meta, i);
-    FriendRows fr(mt, kept_other(mt), c.perCircle);
+    FlatFriends fr(mt, kept_other(mt));
     for (int t = 0; t < fr.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)fr.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
+        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const float4 qj = q[j];
         const F3 r = pi - f3(qj);
         const float r2 = dot(r, r);
@@ -224,9 +225,9 @@ adj_scaling_kernel(DevConsts c, const float4* __restrict__ q, const float* __res
     const uint64_t mt = load_meta(meta, i);
     float ds = 0.0f, gsk = 0.0f;
     F3 S = {0.0f, 0.0f, 0.0f};
-    FriendRows f1(mt, kept_density(mt), c.perCircle);
+    FlatFriends f1(mt, kept_density(mt));
     for (int t = 0; t < f1.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)f1.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
+        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const F3 r = pi - f3(q[j]);
         const float r2 = dot(r, r);
         if (!in_support(c, r2)) continue;
@@ -240,9 +241,9 @@ adj_scaling_kernel(DevConsts c, const float4* __restrict__ q, const float* __res
     const float den = D / c.rho0sq + c.eps, Cc = rho / c.rho0 - 1.0f;
     const float rhob = (-lbar / den) / c.rho0;
     const float Db = lbar * Cc / (den * den) / c.rho0sq;
-    FriendRows f2(mt, kept_density(mt), c.perCircle);
+    FlatFriends f2(mt, kept_density(mt));
     for (int t = 0; t < f2.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)f2.row(t) * n + i], (uint32_t)n, c.err, kErrFriendIndex);
+        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const F3 r = pi - f3(q[j]);
         const float r2 = dot(r, r);
         if (!in_support(c, r2)) continue;

@@ -510,9 +510,12 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     }
     const uint32_t* keys = ctx->keys[ctx->keysIdx];
     const size_t v4 = 16 * (size_t)c.n;
-    // With a tape, the friend lists, the packed (p, lambda) of every
-    // iteration and omega are written straight into the tape's buffers.
-    uint32_t* list = tape ? tape->list : ctx->list;
+    // With a tape, the friends (flat rows), the packed (p, lambda) of every
+    // iteration and omega are written straight into the tape's buffers.  The
+    // circle rows (friends builds 1 and 2), or the staged build's scratch,
+    // stay in ctx->list.
+    uint32_t* list = ctx->list;
+    uint32_t* flat = tape ? tape->list : ctx->flat;
     uint2* meta = tape ? tape->meta : ctx->meta;
     float4* omega = tape ? tape->omega : ctx->omega;
     if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->perm, ctx->perm[ctx->keysIdx], 4 * (size_t)c.n, cudaMemcpyDeviceToDevice, s));
@@ -520,8 +523,10 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     const uint32_t tableKeys = ctx->cellsWords * (uint32_t)(is_batch(ctx) ? ctx->sceneParams.size() : 1);
     pbf::launch_update_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s);
     mark("buildFriendsList");
-    pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, meta, ctx->errWord, ls.friends,
-                              ls.friendsAlgorithm, s);
+    // the flat rows of the kept friends: written by the staged build, else
+    // recorded by the first density pass (or flattened when there is none)
+    bool haveFlat = pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, flat, meta, ctx->errWord,
+                                              ls.friends, ls.friendsAlgorithm, s);
     mark("resetPartList");
     pbf::launch_reset_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s);
     launched += 3;
@@ -530,14 +535,19 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     for (unsigned it = 0; it < iters; ++it) {
         float4* packed = tape ? tape->q[it] : ctx->pred[a ^ 1];
         mark("computeScaling", (int)it);
-        // the first density pass records the friends as flat rows; the passes after it walk those
-        pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, it == 0 ? nullptr : ctx->flat,
-                                    it == 0 ? ctx->flat : nullptr, ls.scaling, ls.balance, s);
+        // the first density pass records the flat rows from circle rows when the build wrote those
+        pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, haveFlat ? flat : nullptr,
+                                    haveFlat ? nullptr : flat, ls.scaling, ls.balance, s);
+        haveFlat = true;
         mark("computeDelta", (int)it);
         pbf::launch_compute_delta(c, b, packed, ctx->pos[sortedPos], ctx->pred[a], ctx->density, list, meta,
                                   it + 1 == iters, tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr,
-                                  ctx->flat, ls.delta, ls.balance, s);
+                                  flat, ls.delta, ls.balance, s);
         launched += 2;
+    }
+    if (!haveFlat) {
+        pbf::launch_flatten_friends(c, list, meta, flat, s);
+        ++launched;
     }
     if (iters == 0) {  // packData with the density buffer as it stands (src/Simulation.cpp:591)
         mark("packData");
@@ -556,11 +566,10 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     }
     if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->v2, ctx->vel[V], v4, cudaMemcpyDeviceToDevice, s));
     mark("applyViscosity");
-    const uint32_t* flatIn = iters > 0 ? ctx->flat : nullptr;  // recorded only when a density pass ran
-    pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, flatIn, ls.viscosity,
+    pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, flat, ls.viscosity,
                                 ls.balance, s);
     mark("applyVorticity");
-    pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, flatIn, ls.vorticity,
+    pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, flat, ls.vorticity,
                                 ls.balance, s);
     launched += 3;
     if (rangeOpen) nvtxRangePop();
@@ -1478,27 +1487,25 @@ int pbf_read_friends(pbf_ctx* ctx, uint32_t* counts, uint32_t* list, int list_sl
     if (rc) return rc;
     if (!ctx->stepped) return fail(ctx, PBF_ERR_STATE, "no substep has run yet");
     PBF_CUDA(ctx, cudaSetDevice(ctx->device));
-    const int n = ctx->n, P = (int)ctx->params.particlesPerCircle;
+    const int n = ctx->n;
     std::vector<uint2> meta(n);
     PBF_CUDA(ctx, cudaMemcpyAsync(meta.data(), ctx->meta, 8 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
-    std::vector<uint32_t> rows;
-    if (list && list_slots > 0) {
-        rows.resize((size_t)ctx->listSlots * n);
-        PBF_CUDA(ctx, cudaMemcpyAsync(rows.data(), ctx->list, 4 * rows.size(), cudaMemcpyDeviceToHost, ctx->stream));
-    }
+    // the kept friends of every particle in order: the flat rows the passes walk
+    const int slots = list ? std::min(list_slots, ctx->listSlots) : 0;
+    std::vector<uint32_t> rows((size_t)std::max(slots, 0) * n);
+    if (slots > 0)
+        PBF_CUDA(ctx, cudaMemcpyAsync(rows.data(), ctx->flat, 4 * rows.size(), cudaMemcpyDeviceToHost, ctx->stream));
     PBF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (int i = 0; i < n; ++i) {
         const uint64_t m = (uint64_t)meta[i].x | ((uint64_t)meta[i].y << 32);
         const int keptL = (int)(m >> 56) & 0xF, keptD = (int)(m >> 60) & 0xF;
-        uint32_t nl = 0, nd = 0, slot = 0;
+        uint32_t nl = 0, nd = 0;
         for (int k = 0; k < keptL; ++k) {
             const uint32_t cnt = (uint32_t)(m >> (7 * k)) & 0x7Fu;
             nl += cnt;
             if (k < keptD) nd += cnt;
-            if (!rows.empty())
-                for (uint32_t f = 0; f < cnt; ++f, ++slot)
-                    if ((int)slot < list_slots) list[(size_t)slot * n + i] = rows[(size_t)(k * P + (int)f) * n + i];
         }
+        for (int t = 0; t < slots && t < (int)nl; ++t) list[(size_t)t * n + i] = rows[(size_t)t * n + i];
         if (counts) { counts[2 * i] = nl; counts[2 * i + 1] = nd; }
     }
     return PBF_OK;

@@ -107,9 +107,13 @@ void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const 
                           float4* posOut, float4* predOut, uint32_t* idsOut, int* err, cudaStream_t s);
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
-// algorithm: LaunchShape::friendsAlgorithm
-void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s);
+// algorithm: LaunchShape::friendsAlgorithm.  Every build writes the circle
+// rows into `list`; none writes the flat rows (the first density pass
+// records them), so the return value, whether `flat` was written, is false.
+bool launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
+                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s);
+// The flat rows from the circle rows, when no density pass records them.
+void launch_flatten_friends(const DevConsts& c, const uint32_t* list, const uint2* meta, uint32_t* flat, cudaStream_t s);
 // flatIn / flatOut (may be NULL): the friends recorded in order as flat rows
 // flat[t * N + i] by the first density pass of a substep (flatOut) and read
 // from there by the passes after it (flatIn) instead of the circle rows.
@@ -154,7 +158,7 @@ int radix_sort_launches(const SortPlan& plan);
 struct AdjointTape {
     int iterations = 0;
     uint32_t* perm = nullptr;      // sorted index k came from perm[k]
-    uint32_t* list = nullptr;      // friend rows of the substep
+    uint32_t* list = nullptr;      // the substep's kept friends as flat rows (friend t of i at t * N + i)
     uint2* meta = nullptr;
     float4* q[64] = {};            // (p^t, lambda^t), t < iterations
     uint8_t* mask = nullptr;       // iterations x N box-clamp decisions (NULL: no clamp)

@@ -975,8 +975,8 @@ void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t k
     reset_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, reinterpret_cast<uint2*>(cells), keyLimit, err);
 }
 
-void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s) {
+bool launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
+                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s) {
     const bool pow2 = (c.grid & (c.grid - 1)) == 0;
     const uint32_t keys = c.grid * (uint32_t)(b.scenes ? b.nscenes : 1);
     const uint2* cellPairs = reinterpret_cast<const uint2*>(cells);
@@ -985,11 +985,29 @@ void launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const
     if (algorithm == 2 && pow2 && c.grid >= 64) {  // one block per 4x4x4-cell brick over all scenes
         auto kb = narrow ? build_friends_brick_kernel<4, true> : build_friends_brick_kernel<4, false>;
         kb<<<keys / 64u, BrickShape<4>::threads, 0, s>>>(c, pred, cellPairs, list, meta, errorWord);
-        return;
+        return false;
     }
     auto k = algorithm == 1 ? build_friends_warp_kernel
                             : (narrow ? build_friends_kernel<2, true> : build_friends_kernel<2, false>);
-    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, reinterpret_cast<const uint2*>(cells), list, meta, errorWord);
+    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, cellPairs, list, meta, errorWord);
+    return false;
+}
+
+namespace {
+// The kept circles' friends as flat rows, in order, from the circle rows,
+// when no density pass records them (zero solver iterations).
+__global__ void flatten_friends_kernel(int n, int perCircle, const uint32_t* __restrict__ list,
+                                       const uint2* __restrict__ meta, uint32_t* __restrict__ flat) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t mt = load_meta(meta, i);
+    FriendRows fr(mt, kept_density(mt), perCircle);
+    for (int t = 0; t < fr.total; ++t) flat[(size_t)t * n + i] = list[(size_t)fr.row(t) * n + i];
+}
+}  // namespace
+
+void launch_flatten_friends(const DevConsts& c, const uint32_t* list, const uint2* meta, uint32_t* flat, cudaStream_t s) {
+    flatten_friends_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c.n, c.perCircle, list, meta, flat);
 }
 
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
