@@ -396,7 +396,7 @@ STAGE_GROUPS = {
     "xsph+vorticity": ("updateVelocities", "applyViscosity", "applyVorticity"),
 }
 
-SHAPE_KEYS = ["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm", "balance"]
+SHAPE_KEYS = ["friends", "scaling", "delta", "viscosity", "vorticity", "friends_algorithm", "balance", "persistent"]
 
 
 def timed_frames(sim, stream, frames: int, sub: int, device_index: int):
@@ -434,6 +434,18 @@ def batched_block(args, single_value: float, device_index: int) -> dict:
         sim.step_async(sub)
     sim.synchronize()
     blocks = sim.autotune(trial_substeps=2)
+    # the same shape with one block per particle tile and with persistent
+    # grids walking the tiles, from the same state (the headline keeps the
+    # autotuner's choice)
+    start_pos, start_vel, _ = sim.read_state()
+    grid_ms = {}
+    for persistent in (0, 1):
+        sim.write_state(start_pos, start_vel)
+        sim.set_launch_shape(list(blocks[:7]) + [persistent])
+        grid_ms["persistent" if persistent else "block_per_tile"], _ = timed_frames(sim, stream, args.batch_steps,
+                                                                                   sub, device_index)
+    sim.write_state(start_pos, start_vel)
+    sim.set_launch_shape(blocks)
     launches0 = sim.launch_count()
     ms, clocks = timed_frames(sim, stream, args.batch_steps, sub, device_index)
     launches = sim.launch_count() - launches0
@@ -463,6 +475,7 @@ def batched_block(args, single_value: float, device_index: int) -> dict:
             "ratio_vs_single_scene": rate / single_value, "single_scene_value": single_value,
             "sequential_value": seq_rate, "ratio_vs_sequential": rate / seq_rate,
             "sequential_steps": args.batch_seq_steps,
+            "grid_ms_per_step": grid_ms,
             "blocks": dict(zip(SHAPE_KEYS, blocks)), "clocks": clocks}
 
 
@@ -877,7 +890,7 @@ def friends_compare(args) -> None:
         sim.step_async(int(params.subSteps))
     sim.synchronize()
     for algorithm in (2, 0):
-        sim.set_launch_shape([256, 128, 128, 128, 128, algorithm, 0])
+        sim.set_launch_shape([256, 128, 128, 128, 128, algorithm, 0, 0])
         sim.Step(1)
     sim.synchronize()
     sim.close()

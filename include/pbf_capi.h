@@ -421,15 +421,19 @@ int pbf_render_read(pbf_ctx* ctx, int which, float* rgba);
    scan from there, for power-of-two GridBufferSize >= 64, else 0), then the balance
    flag (1: the four solver passes hand each block's particles to its threads
    in decreasing order of friend count, so warps walk lists of similar
-   length).  Results do not depend on any of them. */
-#define PBF_LAUNCH_SHAPE_FIELDS 7
+   length), then the persistent flag (1: the four solver passes and friends
+   algorithm 0 launch at most as many blocks as the device keeps resident,
+   and each block walks the tiles of particles grid-stride; blocks never wait
+   on one another).  Results do not depend on any of them. */
+#define PBF_LAUNCH_SHAPE_FIELDS 8
 int pbf_get_launch_shape(pbf_ctx* ctx, int* blocks);
 int pbf_set_launch_shape(pbf_ctx* ctx, const int* blocks);
 
 /* Time `trial_substeps` substeps from the current state for each candidate
    block size (64, 128, 256, 512), the three friends algorithms and both balance
    settings, keep the fastest per kernel (the balance setting by the sum of
-   the solver passes), restore the state (positions, velocities, particle ids
+   the solver passes), then time that shape with and without persistent
+   grids and keep the faster, restore the state (positions, velocities, particle ids
    and the per-stage trackers as they were), and report the choice through
    blocks_out (PBF_LAUNCH_SHAPE_FIELDS ints, may be NULL). */
 int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out);

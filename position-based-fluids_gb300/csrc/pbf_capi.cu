@@ -52,6 +52,7 @@ struct pbf_ctx {
     uint32_t* flat = nullptr;    // the friends of the substep in order, one flat row per position (see enqueue_substep)
     uint2* meta = nullptr;       // per-particle friend counts per circle + kept circles
     int* errWord = nullptr;
+    int* tileCounters = nullptr;  // 2 words per neighbour kernel: its persistent grid's tile counter
     size_t histWords = 0;
     uint32_t cellsWords = 0;  // gridBufSize the cell table was allocated for
     int listSlots = 0;
@@ -493,6 +494,8 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     mark("predictPositions");
     const pbf::Batch b = batch_of(ctx);
     const pbf::LaunchShape& ls = ctx->shape;
+    // persistent grids: each neighbour kernel's pair of tile-counter words
+    auto tiles = [&](int kernel) { return ls.persistent ? ctx->tileCounters + 2 * kernel : nullptr; };
     pbf::launch_predict_keys(c, b, ctx->pos[P], ctx->vel[V], ctx->pred[0], ctx->keys[0], ctx->perm[0], paused, s);
     ++launched;
     int sortedPos = P, sortedPred = 0;
@@ -526,7 +529,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     // the flat rows of the kept friends: written by the staged build, else
     // recorded by the first density pass (or flattened when there is none)
     bool haveFlat = pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, flat, meta, ctx->errWord,
-                                              ls.friends, ls.friendsAlgorithm, s);
+                                              ls.friends, ls.friendsAlgorithm, tiles(0), s);
     mark("resetPartList");
     pbf::launch_reset_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s);
     launched += 3;
@@ -537,12 +540,12 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
         mark("computeScaling", (int)it);
         // the first density pass records the flat rows from circle rows when the build wrote those
         pbf::launch_compute_scaling(c, ctx->pred[a], packed, ctx->density, list, meta, haveFlat ? flat : nullptr,
-                                    haveFlat ? nullptr : flat, ls.scaling, ls.balance, s);
+                                    haveFlat ? nullptr : flat, ls.scaling, ls.balance, tiles(1), s);
         haveFlat = true;
         mark("computeDelta", (int)it);
         pbf::launch_compute_delta(c, b, packed, ctx->pos[sortedPos], ctx->pred[a], ctx->density, list, meta,
                                   it + 1 == iters, tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr,
-                                  flat, ls.delta, ls.balance, s);
+                                  flat, ls.delta, ls.balance, tiles(2), s);
         launched += 2;
     }
     if (!haveFlat) {
@@ -567,10 +570,10 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->v2, ctx->vel[V], v4, cudaMemcpyDeviceToDevice, s));
     mark("applyViscosity");
     pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, flat, ls.viscosity,
-                                ls.balance, s);
+                                ls.balance, tiles(3), s);
     mark("applyVorticity");
     pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, flat, ls.vorticity,
-                                ls.balance, s);
+                                ls.balance, tiles(4), s);
     launched += 3;
     if (rangeOpen) nvtxRangePop();
     if (ctx->readVel) PBF_CUDA(ctx, cudaMemcpyAsync(ctx->readVel, ctx->vel[V], v4, cudaMemcpyDeviceToHost, s));
@@ -860,6 +863,8 @@ int pbf_create(const PbfParameters* params, int device, pbf_ctx** out) {
     // [0]: the error word; [1]: the sticky "irregular coordinate" flag of the exact quotients
     PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->errWord, 2 * sizeof(int)));
     PBF_CUDA(nullptr, cudaMemset(ctx->errWord, 0, 2 * sizeof(int)));
+    PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->tileCounters, 10 * sizeof(int)));
+    PBF_CUDA(nullptr, cudaMemset(ctx->tileCounters, 0, 10 * sizeof(int)));
     *out = ctx.release();
     return PBF_OK;
 }
@@ -874,7 +879,7 @@ int pbf_destroy(pbf_ctx* ctx) {
         dev_free(ctx->keys[k]); dev_free(ctx->perm[k]);
     }
     dev_free(ctx->omega); dev_free(ctx->density); dev_free(ctx->hist); dev_free(ctx->cells);
-    dev_free(ctx->list); dev_free(ctx->flat); dev_free(ctx->meta); dev_free(ctx->errWord);
+    dev_free(ctx->list); dev_free(ctx->flat); dev_free(ctx->meta); dev_free(ctx->errWord); dev_free(ctx->tileCounters);
     dev_free(ctx->scenes); dev_free(ctx->sceneOf); dev_free(ctx->ids); dev_free(ctx->idsTmp);
     dev_free(ctx->quadsDev); dev_free(ctx->maskDev); dev_free(ctx->waveDev);
     if (ctx->timingAnchor) cudaEventDestroy(ctx->timingAnchor);
@@ -1589,6 +1594,7 @@ int pbf_get_launch_shape(pbf_ctx* ctx, int* blocks) {
     blocks[0] = s.friends; blocks[1] = s.scaling; blocks[2] = s.delta; blocks[3] = s.viscosity; blocks[4] = s.vorticity;
     blocks[5] = s.friendsAlgorithm;
     blocks[6] = s.balance;
+    blocks[7] = s.persistent;
     return PBF_OK;
 }
 
@@ -1599,9 +1605,11 @@ int pbf_set_launch_shape(pbf_ctx* ctx, const int* blocks) {
             return fail(ctx, PBF_ERR_INVALID, "block sizes must be multiples of 32 in [32, 512]");
     if (blocks[5] < 0 || blocks[5] > 2) return fail(ctx, PBF_ERR_INVALID, "the friends algorithm is 0, 1 or 2");
     if (blocks[6] != 0 && blocks[6] != 1) return fail(ctx, PBF_ERR_INVALID, "the balance flag is 0 or 1");
+    if (blocks[7] != 0 && blocks[7] != 1) return fail(ctx, PBF_ERR_INVALID, "the persistent flag is 0 or 1");
     ctx->shape.friends = blocks[0]; ctx->shape.scaling = blocks[1]; ctx->shape.delta = blocks[2];
     ctx->shape.viscosity = blocks[3]; ctx->shape.vorticity = blocks[4]; ctx->shape.friendsAlgorithm = blocks[5];
     ctx->shape.balance = blocks[6];
+    ctx->shape.persistent = blocks[7];
     drop_graph(ctx);
     return PBF_OK;
 }
@@ -1675,7 +1683,7 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
     for (int trial = 0; trial < 24; ++trial) {
         // block size x friends algorithm (3) x balanced thread map (2)
         const int cand = candidates[trial % 4], algo = (trial / 4) % 3, bal = trial / 12;
-        ctx->shape = pbf::LaunchShape{cand, cand, cand, cand, cand, algo, bal};
+        ctx->shape = pbf::LaunchShape{cand, cand, cand, cand, cand, algo, bal, 0};
         ctx->stageNames.clear();
         ctx->stageMs.clear();
         StageClock clock{ctx, {}};
@@ -1697,6 +1705,27 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
     const int balance = sum[1] <= sum[0] ? 1 : 0;
     int choice[5] = {friendsBlock, solverBlock[balance][0], solverBlock[balance][1], solverBlock[balance][2],
                      solverBlock[balance][3]};
+    // then one block per tile against a persistent grid walking the tiles,
+    // with that shape: the smaller sum of the five neighbour stages (the
+    // better of two trials each, alternated)
+    float persistMs[2] = {1e30f, 1e30f};
+    for (int trial = 0; trial < 4 && rc == PBF_OK; ++trial) {
+        const int pers = trial & 1;
+        ctx->shape = pbf::LaunchShape{choice[0], choice[1], choice[2], choice[3], choice[4], algorithm, balance, pers};
+        ctx->stageNames.clear();
+        ctx->stageMs.clear();
+        StageClock clock{ctx, {}};
+        for (int k = 0; k < trial_substeps && rc == PBF_OK; ++k) rc = enqueue_substep(ctx, &clock);
+        if (rc == PBF_OK) rc = clock.finish();
+        restore();
+        if (rc != PBF_OK) break;
+        float ms = 0.0f;
+        for (int q = 0; q < 5; ++q)
+            for (size_t k = 0; k < ctx->stageNames.size(); ++k)
+                if (ctx->stageNames[k] == names[q]) ms += ctx->stageMs[k];
+        persistMs[pers] = std::min(persistMs[pers], ms);
+    }
+    const int persistent = persistMs[1] < persistMs[0] ? 1 : 0;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e == cudaSuccess) e = restoreErr;
     release();
@@ -1709,11 +1738,12 @@ int pbf_autotune(pbf_ctx* ctx, int trial_substeps, int* blocks_out) {
     drop_graph(ctx);
     if (rc != PBF_OK) { ctx->shape = shape0; return rc; }
     if (e != cudaSuccess) { ctx->shape = shape0; return fail(ctx, PBF_ERR_CUDA, std::string("pbf_autotune: ") + cudaGetErrorString(e)); }
-    ctx->shape = pbf::LaunchShape{choice[0], choice[1], choice[2], choice[3], choice[4], algorithm, balance};
+    ctx->shape = pbf::LaunchShape{choice[0], choice[1], choice[2], choice[3], choice[4], algorithm, balance, persistent};
     if (blocks_out) {
         for (int q = 0; q < 5; ++q) blocks_out[q] = choice[q];
         blocks_out[5] = algorithm;
         blocks_out[6] = balance;
+        blocks_out[7] = persistent;
     }
     return read_error_word(ctx);
 }

@@ -93,6 +93,8 @@ struct LaunchShape {
     int friendsAlgorithm = 0;  // 0: one thread scans per particle; 1: warp-cooperative runs;
                                // 2: 4x4x4-cell bricks streamed through shared memory
     int balance = 0;           // solver passes: threads take the block's particles by friend count
+    int persistent = 0;        // the scan build and the solver passes: a grid of the resident
+                               // blocks walks the particle tiles grid-stride (no waits between blocks)
 };
 constexpr int kMaxBlock = 512;
 
@@ -107,11 +109,15 @@ void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const 
                           float4* posOut, float4* predOut, uint32_t* idsOut, int* err, cudaStream_t s);
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
+// tileCounter (two device words, zero between launches; NULL for one block
+// per tile of particles): the neighbour passes' persistent grid, whose
+// blocks take the tiles from it (LaunchShape::persistent).
 // algorithm: LaunchShape::friendsAlgorithm.  Every build writes the circle
 // rows into `list`; none writes the flat rows (the first density pass
 // records them), so the return value, whether `flat` was written, is false.
 bool launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s);
+                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, int* tileCounter,
+                          cudaStream_t s);
 // The flat rows from the circle rows, when no density pass records them.
 void launch_flatten_friends(const DevConsts& c, const uint32_t* list, const uint2* meta, uint32_t* flat, cudaStream_t s);
 // flatIn / flatOut (may be NULL): the friends recorded in order as flat rows
@@ -119,20 +125,20 @@ void launch_flatten_friends(const DevConsts& c, const uint32_t* list, const uint
 // from there by the passes after it (flatIn) instead of the circle rows.
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
                             const uint32_t* list, const uint2* meta, const uint32_t* flatIn, uint32_t* flatOut,
-                            int block, int balance, cudaStream_t s);
+                            int block, int balance, int* tileCounter, cudaStream_t s);
 // posPrev: the sorted positions, read only by the force planes.
 void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, const float4* posPrev,
                           float4* predOut, const float* density, const uint32_t* list, const uint2* meta,
                           int lastIteration, uint8_t* clampMask, const uint32_t* flatIn, int block, int balance,
-                          cudaStream_t s);
+                          int* tileCounter, cudaStream_t s);
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
                               float4* vel, const uint32_t* idsIn, uint32_t* idsOut, cudaStream_t s);
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
                             float4* omega, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
-                            int balance, cudaStream_t s);
+                            int balance, int* tileCounter, cudaStream_t s);
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
                             float4* velOut, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
-                            int balance, cudaStream_t s);
+                            int balance, int* tileCounter, cudaStream_t s);
 
 // ---- radix sort (pbf_sort.cu) ----
 struct SortPlan {

@@ -262,12 +262,15 @@ __device__ __forceinline__ void friends_scan_global(const DevConsts& c, uint32_t
 template <int U, bool Narrow>
 __global__ void __launch_bounds__(kMaxBlock)
 build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const uint2* __restrict__ cells,
-                     uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
-    FriendCircles<Narrow> fc(c, list, i, pred[i]);
-    friends_scan_global<U>(c, key_base(b, i), pred, cells, err, fc);
-    fc.finish(meta);
+                     uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err, int tiles,
+                     int* tileCounter) {
+    for_tiles(tiles, tileCounter, [&](int tile) {
+        const int i = tile * (int)blockDim.x + (int)threadIdx.x;
+        if (i >= c.n) return;
+        FriendCircles<Narrow> fc(c, list, i, pred[i]);
+        friends_scan_global<U>(c, key_base(b, i), pred, cells, err, fc);
+        fc.finish(meta);
+    });
 }
 
 // The same lists with the candidates streamed through shared memory, one
@@ -527,11 +530,11 @@ build_friends_warp_kernel(DevConsts c, Batch b, const float4* __restrict__ pred,
 // sort in shared memory over the kept-circle count (saturated at 255), ties
 // in any order.  Every thread of the block must call it (it synchronises);
 // returns the particle index, or -1 for threads beyond the block's particles.
-__device__ __forceinline__ int balanced_particle(const uint2* __restrict__ meta, int n, bool densityPass) {
+__device__ __forceinline__ int balanced_particle(const uint2* __restrict__ meta, int n, bool densityPass, int tile) {
     __shared__ uint32_t bins[256];
     __shared__ int order[kMaxBlock];
     const int t = threadIdx.x;
-    const int i = blockIdx.x * blockDim.x + t;
+    const int i = tile * blockDim.x + t;
     for (int k = t; k < 256; k += blockDim.x) bins[k] = 0u;
     __syncthreads();
     int key = -1;
@@ -561,8 +564,38 @@ __device__ __forceinline__ int balanced_particle(const uint2* __restrict__ meta,
     __syncthreads();
     if (key >= 0) order[atomicAdd(&bins[key], 1u)] = i;
     __syncthreads();
-    const int valid = min(n - (int)(blockIdx.x * blockDim.x), (int)blockDim.x);
+    const int valid = min(n - tile * (int)blockDim.x, (int)blockDim.x);
     return t < valid ? order[t] : -1;
+}
+
+// ---------------------------------------------------- tiles of a launch --
+// A launch covers `tiles` tiles of blockDim particles.  With tiles == 0, one
+// block per tile (tile = blockIdx.x).  Otherwise a persistent grid of at
+// most the resident blocks takes the tiles in order from counter[0], one
+// atomic per tile, so busy SMs take fewer tiles; no block waits on another.
+// The last block to find the tiles exhausted resets counter[0] and
+// counter[1] to 0 for the next launch on the stream.  Every thread of a
+// block runs every tile the block takes (the balanced thread map
+// synchronises).
+template <typename F>
+__device__ __forceinline__ void for_tiles(int tiles, int* counter, F body) {
+    if (tiles == 0) {
+        body((int)blockIdx.x);
+        return;
+    }
+    __shared__ int nextTile;
+    while (true) {
+        if (threadIdx.x == 0) nextTile = atomicAdd(&counter[0], 1);
+        __syncthreads();
+        const int t = nextTile;
+        __syncthreads();
+        if (t >= tiles) break;
+        body(t);
+    }
+    if (threadIdx.x == 0 && atomicAdd(&counter[1], 1) == (int)gridDim.x - 1) {
+        counter[0] = 0;
+        counter[1] = 0;
+    }
 }
 
 // -------------------------------------------------------------- scaling --
@@ -583,9 +616,10 @@ template <bool R, bool B, int W, bool Q>
 __device__ __forceinline__ void compute_scaling_body(const DevConsts& c, const float4* __restrict__ pred,
                                                      float4* __restrict__ predPacked, float* __restrict__ density,
                                                      const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
-                                                     const uint32_t* __restrict__ flatIn, uint32_t* __restrict__ flatOut) {
+                                                     const uint32_t* __restrict__ flatIn, uint32_t* __restrict__ flatOut,
+                                                     int tile) {
     const int n = c.n;
-    const int i = B ? balanced_particle(meta, n, true) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = B ? balanced_particle(meta, n, true, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
     if (i < 0 || i >= n) return;
     const float4 pi = pred[i];
     const uint64_t mt = load_meta(meta, i);
@@ -647,9 +681,12 @@ __global__ void __launch_bounds__(kMaxBlock)
 compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __restrict__ predPacked,
                        float* __restrict__ density, const uint32_t* __restrict__ list,
                        const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn,
-                       uint32_t* __restrict__ flatOut) {
-    if (!R && exact_quotients(c)) compute_scaling_body<R, B, W, true>(c, pred, predPacked, density, list, meta, flatIn, flatOut);
-    else compute_scaling_body<R, B, W, false>(c, pred, predPacked, density, list, meta, flatIn, flatOut);
+                       uint32_t* __restrict__ flatOut, int tiles, int* tileCounter) {
+    const bool q = !R && exact_quotients(c);
+    for_tiles(tiles, tileCounter, [&](int tile) {
+        if (q) compute_scaling_body<R, B, W, true>(c, pred, predPacked, density, list, meta, flatIn, flatOut, tile);
+        else compute_scaling_body<R, B, W, false>(c, pred, predPacked, density, list, meta, flatIn, flatOut, tile);
+    });
 }
 
 // ---------------------------------------------------------------- delta --
@@ -662,9 +699,10 @@ __device__ __forceinline__ void compute_delta_body(const DevConsts& c, const Bat
                                                    const float4* __restrict__ posPrev, float4* __restrict__ predOut,
                                                    const float* __restrict__ density, const uint32_t* __restrict__ list,
                                                    const uint2* __restrict__ meta, int lastIteration,
-                                                   uint8_t* __restrict__ clampMask, const uint32_t* __restrict__ flatIn) {
+                                                   uint8_t* __restrict__ clampMask, const uint32_t* __restrict__ flatIn,
+                                                   int tile) {
     const int n = c.n;
-    const int i = B ? balanced_particle(meta, n, false) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = B ? balanced_particle(meta, n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
     if (i < 0 || i >= n) return;
     const float4 pi = pp[i];
     const uint64_t mt = load_meta(meta, i);
@@ -758,11 +796,12 @@ __global__ void __launch_bounds__(kMaxBlock)
 compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const float4* __restrict__ posPrev,
                      float4* __restrict__ predOut, const float* __restrict__ density, const uint32_t* __restrict__ list,
                      const uint2* __restrict__ meta, int lastIteration, uint8_t* __restrict__ clampMask,
-                     const uint32_t* __restrict__ flatIn) {
-    if (!R && exact_quotients(c))
-        compute_delta_body<R, B, W, true>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn);
-    else
-        compute_delta_body<R, B, W, false>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn);
+                     const uint32_t* __restrict__ flatIn, int tiles, int* tileCounter) {
+    const bool q = !R && exact_quotients(c);
+    for_tiles(tiles, tileCounter, [&](int tile) {
+        if (q) compute_delta_body<R, B, W, true>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn, tile);
+        else compute_delta_body<R, B, W, false>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn, tile);
+    });
 }
 
 // ----------------------------------------------------------- velocities --
@@ -792,9 +831,10 @@ template <bool R, bool B, int W, bool Q>
 __device__ __forceinline__ void apply_viscosity_body(const DevConsts& c, const Batch& b, const float4* __restrict__ pred,
                                                      const float4* __restrict__ velIn, float4* __restrict__ velOut,
                                                      float4* __restrict__ omega, const uint32_t* __restrict__ list,
-                                                     const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn) {
+                                                     const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn,
+                                                     int tile) {
     const int n = c.n;
-    const int i = B ? balanced_particle(meta, n, false) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = B ? balanced_particle(meta, n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
     if (i < 0 || i >= n) return;
     const float4 pi = pred[i], vi = velIn[i];
     const uint64_t mt = load_meta(meta, i);
@@ -858,9 +898,12 @@ __global__ void __launch_bounds__(kMaxBlock)
 apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const float4* __restrict__ velIn,
                        float4* __restrict__ velOut, float4* __restrict__ omega,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
-                       const uint32_t* __restrict__ flatIn) {
-    if (!R && exact_quotients(c)) apply_viscosity_body<R, B, W, true>(c, b, pred, velIn, velOut, omega, list, meta, flatIn);
-    else apply_viscosity_body<R, B, W, false>(c, b, pred, velIn, velOut, omega, list, meta, flatIn);
+                       const uint32_t* __restrict__ flatIn, int tiles, int* tileCounter) {
+    const bool q = !R && exact_quotients(c);
+    for_tiles(tiles, tileCounter, [&](int tile) {
+        if (q) apply_viscosity_body<R, B, W, true>(c, b, pred, velIn, velOut, omega, list, meta, flatIn, tile);
+        else apply_viscosity_body<R, B, W, false>(c, b, pred, velIn, velOut, omega, list, meta, flatIn, tile);
+    });
 }
 
 // apply_vorticity.cl:12-86; |omega_j| is read from omega.w (apply_viscosity).
@@ -868,9 +911,10 @@ template <bool R, bool B, int W, bool Q>
 __device__ __forceinline__ void apply_vorticity_body(const DevConsts& c, const float4* __restrict__ pred,
                                                      const float4* __restrict__ omega, const float4* __restrict__ velIn,
                                                      float4* __restrict__ velOut, const uint32_t* __restrict__ list,
-                                                     const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn) {
+                                                     const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn,
+                                                     int tile) {
     const int n = c.n;
-    const int i = B ? balanced_particle(meta, n, false) : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = B ? balanced_particle(meta, n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
     if (i < 0 || i >= n) return;
     const float4 pi = pred[i];
     const uint64_t mt = load_meta(meta, i);
@@ -944,9 +988,12 @@ __global__ void __launch_bounds__(kMaxBlock)
 apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
                        const float4* __restrict__ velIn, float4* __restrict__ velOut,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
-                       const uint32_t* __restrict__ flatIn) {
-    if (!R && exact_quotients(c)) apply_vorticity_body<R, B, W, true>(c, pred, omega, velIn, velOut, list, meta, flatIn);
-    else apply_vorticity_body<R, B, W, false>(c, pred, omega, velIn, velOut, list, meta, flatIn);
+                       const uint32_t* __restrict__ flatIn, int tiles, int* tileCounter) {
+    const bool q = !R && exact_quotients(c);
+    for_tiles(tiles, tileCounter, [&](int tile) {
+        if (q) apply_vorticity_body<R, B, W, true>(c, pred, omega, velIn, velOut, list, meta, flatIn, tile);
+        else apply_vorticity_body<R, B, W, false>(c, pred, omega, velIn, velOut, list, meta, flatIn, tile);
+    });
 }
 
 }  // namespace
@@ -975,8 +1022,36 @@ void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t k
     reset_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, reinterpret_cast<uint2*>(cells), keyLimit, err);
 }
 
+// Grid of a neighbour pass: one block per tile of `block` particles, or
+// (persistent) at most as many blocks as the device keeps resident, which
+// then take the tiles from a counter (*tiles receives their count; 0 for one
+// block per tile).  A launcher's tileCounter (two words, zero between
+// launches) selects the persistent grid; NULL, one block per tile.
+template <typename K>
+unsigned grid_for_tiles(K kernel, int n, int block, bool persistent, int* tiles) {
+    const unsigned all = blocks_for(n, block);
+    *tiles = 0;
+    if (!persistent) return all;  // no tile counter: one block per tile
+    static int sms[64] = {};  // per device, filled on first use
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return all;
+    if (!sms[dev]) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    int resident = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kernel, block, 0) != cudaSuccess || resident < 1 ||
+        sms[dev] < 1) {
+        cudaGetLastError();
+        return all;
+    }
+    const unsigned cap = (unsigned)resident * (unsigned)sms[dev];
+    if (all <= cap) return all;
+    *tiles = (int)all;
+    return cap;
+}
+
 bool launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s) {
+                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, int* tileCounter,
+                          cudaStream_t s) {
     const bool pow2 = (c.grid & (c.grid - 1)) == 0;
     const uint32_t keys = c.grid * (uint32_t)(b.scenes ? b.nscenes : 1);
     const uint2* cellPairs = reinterpret_cast<const uint2*>(cells);
@@ -987,9 +1062,14 @@ bool launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const
         kb<<<keys / 64u, BrickShape<4>::threads, 0, s>>>(c, pred, cellPairs, list, meta, errorWord);
         return false;
     }
-    auto k = algorithm == 1 ? build_friends_warp_kernel
-                            : (narrow ? build_friends_kernel<2, true> : build_friends_kernel<2, false>);
-    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, cellPairs, list, meta, errorWord);
+    if (algorithm == 1) {
+        build_friends_warp_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, cellPairs, list, meta, errorWord);
+        return false;
+    }
+    auto k = narrow ? build_friends_kernel<2, true> : build_friends_kernel<2, false>;
+    int tiles = 0;
+    const unsigned grid = grid_for_tiles(k, c.n, block, tileCounter != nullptr, &tiles);
+    k<<<grid, block, 0, s>>>(c, b, pred, cellPairs, list, meta, errorWord, tiles, tileCounter);
     return false;
 }
 
@@ -1010,33 +1090,32 @@ void launch_flatten_friends(const DevConsts& c, const uint32_t* list, const uint
     flatten_friends_kernel<<<blocks_for(c.n), kBlock, 0, s>>>(c.n, c.perCircle, list, meta, flat);
 }
 
+// The first density pass of a substep records the flat rows from the circle
+// rows (flatOut); the other passes walk the flat rows (flatIn).
 void launch_compute_scaling(const DevConsts& c, const float4* pred, float4* predPacked, float* density,
                             const uint32_t* list, const uint2* meta, const uint32_t* flatIn, uint32_t* flatOut,
-                            int block, int balance, cudaStream_t s) {
-    const int w = flatOut ? kWalkRecord : (flatIn ? kWalkFlat : kWalkRows);
-    auto pick = [w](auto rows, auto record, auto flat) { return w == kWalkFlat ? flat : (w == kWalkRecord ? record : rows); };
-    auto k = c.relaxed ? (balance ? pick(compute_scaling_kernel<true, true, kWalkRows>, compute_scaling_kernel<true, true, kWalkRecord>,
-                                         compute_scaling_kernel<true, true, kWalkFlat>)
-                                  : pick(compute_scaling_kernel<true, false, kWalkRows>, compute_scaling_kernel<true, false, kWalkRecord>,
-                                         compute_scaling_kernel<true, false, kWalkFlat>))
-                       : (balance ? pick(compute_scaling_kernel<false, true, kWalkRows>, compute_scaling_kernel<false, true, kWalkRecord>,
-                                         compute_scaling_kernel<false, true, kWalkFlat>)
-                                  : pick(compute_scaling_kernel<false, false, kWalkRows>, compute_scaling_kernel<false, false, kWalkRecord>,
-                                         compute_scaling_kernel<false, false, kWalkFlat>));
-    k<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, predPacked, density, list, meta, flatIn, flatOut);
+                            int block, int balance, int* tileCounter, cudaStream_t s) {
+    const bool record = flatOut != nullptr;
+    auto pick = [record](auto rec, auto flat) { return record ? rec : flat; };
+    auto k = c.relaxed ? (balance ? pick(compute_scaling_kernel<true, true, kWalkRecord>, compute_scaling_kernel<true, true, kWalkFlat>)
+                                  : pick(compute_scaling_kernel<true, false, kWalkRecord>, compute_scaling_kernel<true, false, kWalkFlat>))
+                       : (balance ? pick(compute_scaling_kernel<false, true, kWalkRecord>, compute_scaling_kernel<false, true, kWalkFlat>)
+                                  : pick(compute_scaling_kernel<false, false, kWalkRecord>, compute_scaling_kernel<false, false, kWalkFlat>));
+    int tiles = 0;
+    const unsigned grid = grid_for_tiles(k, c.n, block, tileCounter != nullptr, &tiles);
+    k<<<grid, block, 0, s>>>(c, pred, predPacked, density, list, meta, flatIn, flatOut, tiles, tileCounter);
 }
 
 void launch_compute_delta(const DevConsts& c, Batch b, const float4* predPacked, const float4* posPrev,
                           float4* predOut, const float* density, const uint32_t* list, const uint2* meta,
                           int lastIteration, uint8_t* clampMask, const uint32_t* flatIn, int block, int balance,
-                          cudaStream_t s) {
-    auto pick = [flatIn](auto rows, auto flat) { return flatIn ? flat : rows; };
-    auto k = c.relaxed ? (balance ? pick(compute_delta_kernel<true, true, kWalkRows>, compute_delta_kernel<true, true, kWalkFlat>)
-                                  : pick(compute_delta_kernel<true, false, kWalkRows>, compute_delta_kernel<true, false, kWalkFlat>))
-                       : (balance ? pick(compute_delta_kernel<false, true, kWalkRows>, compute_delta_kernel<false, true, kWalkFlat>)
-                                  : pick(compute_delta_kernel<false, false, kWalkRows>, compute_delta_kernel<false, false, kWalkFlat>));
-    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, predPacked, posPrev, predOut, density, list, meta, lastIteration,
-                                               clampMask, flatIn);
+                          int* tileCounter, cudaStream_t s) {
+    auto k = c.relaxed ? (balance ? compute_delta_kernel<true, true, kWalkFlat> : compute_delta_kernel<true, false, kWalkFlat>)
+                       : (balance ? compute_delta_kernel<false, true, kWalkFlat> : compute_delta_kernel<false, false, kWalkFlat>);
+    int tiles = 0;
+    const unsigned grid = grid_for_tiles(k, c.n, block, tileCounter != nullptr, &tiles);
+    k<<<grid, block, 0, s>>>(c, b, predPacked, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn,
+                             tiles, tileCounter);
 }
 
 void launch_update_velocities(const DevConsts& c, const float4* pred, const float4* posIn, float4* posOut,
@@ -1046,24 +1125,22 @@ void launch_update_velocities(const DevConsts& c, const float4* pred, const floa
 
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
                             float4* omega, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
-                            int balance, cudaStream_t s) {
-    auto pick = [flatIn](auto rows, auto flat) { return flatIn ? flat : rows; };
-    auto k = c.relaxed ? (balance ? pick(apply_viscosity_kernel<true, true, kWalkRows>, apply_viscosity_kernel<true, true, kWalkFlat>)
-                                  : pick(apply_viscosity_kernel<true, false, kWalkRows>, apply_viscosity_kernel<true, false, kWalkFlat>))
-                       : (balance ? pick(apply_viscosity_kernel<false, true, kWalkRows>, apply_viscosity_kernel<false, true, kWalkFlat>)
-                                  : pick(apply_viscosity_kernel<false, false, kWalkRows>, apply_viscosity_kernel<false, false, kWalkFlat>));
-    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, velIn, velOut, omega, list, meta, flatIn);
+                            int balance, int* tileCounter, cudaStream_t s) {
+    auto k = c.relaxed ? (balance ? apply_viscosity_kernel<true, true, kWalkFlat> : apply_viscosity_kernel<true, false, kWalkFlat>)
+                       : (balance ? apply_viscosity_kernel<false, true, kWalkFlat> : apply_viscosity_kernel<false, false, kWalkFlat>);
+    int tiles = 0;
+    const unsigned grid = grid_for_tiles(k, c.n, block, tileCounter != nullptr, &tiles);
+    k<<<grid, block, 0, s>>>(c, b, pred, velIn, velOut, omega, list, meta, flatIn, tiles, tileCounter);
 }
 
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
                             float4* velOut, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
-                            int balance, cudaStream_t s) {
-    auto pick = [flatIn](auto rows, auto flat) { return flatIn ? flat : rows; };
-    auto k = c.relaxed ? (balance ? pick(apply_vorticity_kernel<true, true, kWalkRows>, apply_vorticity_kernel<true, true, kWalkFlat>)
-                                  : pick(apply_vorticity_kernel<true, false, kWalkRows>, apply_vorticity_kernel<true, false, kWalkFlat>))
-                       : (balance ? pick(apply_vorticity_kernel<false, true, kWalkRows>, apply_vorticity_kernel<false, true, kWalkFlat>)
-                                  : pick(apply_vorticity_kernel<false, false, kWalkRows>, apply_vorticity_kernel<false, false, kWalkFlat>));
-    k<<<blocks_for(c.n, block), block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta, flatIn);
+                            int balance, int* tileCounter, cudaStream_t s) {
+    auto k = c.relaxed ? (balance ? apply_vorticity_kernel<true, true, kWalkFlat> : apply_vorticity_kernel<true, false, kWalkFlat>)
+                       : (balance ? apply_vorticity_kernel<false, true, kWalkFlat> : apply_vorticity_kernel<false, false, kWalkFlat>);
+    int tiles = 0;
+    const unsigned grid = grid_for_tiles(k, c.n, block, tileCounter != nullptr, &tiles);
+    k<<<grid, block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta, flatIn, tiles, tileCounter);
 }
 
 }  // namespace pbf

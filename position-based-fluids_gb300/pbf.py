@@ -32,6 +32,7 @@ PBF_ERR_NO_DEVICE = -6
 MAX_PARTICLES = 1 << 26
 
 PAD_KEY = 2147483646
+LAUNCH_SHAPE_FIELDS = 8  # PBF_LAUNCH_SHAPE_FIELDS
 EMPTY = 0xFFFFFFFF
 
 
@@ -499,18 +500,20 @@ class Simulation:
         return out
 
     def launch_shape(self) -> list:
-        b = (c_int * 7)()
+        """[friends, scaling, delta, viscosity, vorticity block sizes,
+        friends algorithm, balance, persistent] (PBF_LAUNCH_SHAPE_FIELDS)."""
+        b = (c_int * LAUNCH_SHAPE_FIELDS)()
         _check(self.lib.pbf_get_launch_shape(self._ctx, b), self._ctx)
         return list(b)
 
     def set_launch_shape(self, blocks) -> None:
         blocks = list(blocks)
         blocks += self.launch_shape()[len(blocks):]
-        b = (c_int * 7)(*blocks)
+        b = (c_int * LAUNCH_SHAPE_FIELDS)(*blocks)
         _check(self.lib.pbf_set_launch_shape(self._ctx, b), self._ctx)
 
     def autotune(self, trial_substeps: int = 2) -> list:
-        b = (c_int * 7)()
+        b = (c_int * LAUNCH_SHAPE_FIELDS)()
         _check(self.lib.pbf_autotune(self._ctx, trial_substeps, b), self._ctx)
         return list(b)
 

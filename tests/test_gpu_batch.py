@@ -60,13 +60,13 @@ def test_autotune_keeps_results_and_state(pbf_mod, cuda_device):
         b.Step(1)
         blocks = b.autotune(trial_substeps=1)
         assert b.launch_shape() == blocks and all(x in (64, 128, 256, 512) for x in blocks[:5])
-        assert blocks[5] in (0, 1, 2) and blocks[6] in (0, 1)
+        assert blocks[5] in (0, 1, 2) and blocks[6] in (0, 1) and blocks[7] in (0, 1)
         a.Step(2)
         b.Step(2)
         for x, y in zip(a.read_state(), b.read_state()):
             assert _same(x, y)
         assert np.array_equal(a.read_ids(), b.read_ids())  # the trials' permutations are undone too
-        b.set_launch_shape([96, 160, 224, 288, 352, (blocks[5] + 1) % 3, 1 - blocks[6]])  # another algorithm
+        b.set_launch_shape([96, 160, 224, 288, 352, (blocks[5] + 1) % 3, 1 - blocks[6], 1 - blocks[7]])  # another shape
         b.Step(1)
         a.Step(1)
         for x, y in zip(a.read_state(), b.read_state()):

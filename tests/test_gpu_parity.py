@@ -202,6 +202,23 @@ def test_tiny_coordinates_bit_exact(pbf_mod, oracle_mod, cuda_device):
     assert_same("pred", gpr, opr)
 
 
+def test_persistent_grids_bit_identical(pbf_mod, cuda_device):
+    """Persistent grids (at most the resident blocks, walking the particle
+    tiles grid-stride) against one block per tile: the 1M dam break with
+    64-thread blocks has 16,384 tiles, more than a GB300 keeps resident, so
+    every block walks several tiles; with and without the balanced thread map."""
+    params, pos, vel = pbf_mod.make_scene("dam_break_1m")
+    for balance in (0, 1):
+        out = []
+        for persistent in (0, 1):
+            with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+                sim.set_launch_shape([64, 64, 64, 64, 64, 0, balance, persistent])
+                sim.Step(4)
+                out.append(sim.read_state())
+        for name, x, y in zip(("pos", "vel", "pred"), out[0], out[1]):
+            assert_same(f"{name} (balance {balance})", y, x)
+
+
 def test_graph_and_eager_paths_agree(pbf_mod, cuda_device):
     params, pos, vel = scene(pbf_mod, (20, 20, 20))
     a = run_gpu(pbf_mod, params, pos, vel, 5, cuda_device, graph=True)
