@@ -421,8 +421,8 @@ int pbf_render_read(pbf_ctx* ctx, int which, float* rgba);
    scan from there, for power-of-two GridBufferSize >= 64, else 0), then the balance
    flag (1: the four solver passes hand each block's particles to its threads
    in decreasing order of friend count, so warps walk lists of similar
-   length), then the persistent flag (1: the four solver passes and friends
-   algorithm 0 launch at most as many blocks as the device keeps resident,
+   length), then the persistent flag (1: the four solver passes launch at
+   most as many blocks as the device keeps resident,
    and each block walks the tiles of particles grid-stride; blocks never wait
    on one another).  Results do not depend on any of them. */
 #define PBF_LAUNCH_SHAPE_FIELDS 8

@@ -529,7 +529,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     // the flat rows of the kept friends: written by the staged build, else
     // recorded by the first density pass (or flattened when there is none)
     bool haveFlat = pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, flat, meta, ctx->errWord,
-                                              ls.friends, ls.friendsAlgorithm, tiles(0), s);
+                                              ls.friends, ls.friendsAlgorithm, s);
     mark("resetPartList");
     pbf::launch_reset_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s);
     launched += 3;

@@ -93,8 +93,8 @@ struct LaunchShape {
     int friendsAlgorithm = 0;  // 0: one thread scans per particle; 1: warp-cooperative runs;
                                // 2: 4x4x4-cell bricks streamed through shared memory
     int balance = 0;           // solver passes: threads take the block's particles by friend count
-    int persistent = 0;        // the scan build and the solver passes: a grid of the resident
-                               // blocks walks the particle tiles grid-stride (no waits between blocks)
+    int persistent = 0;        // the four solver passes: a grid of the resident blocks takes
+                               // the particle tiles from a counter (no waits between blocks)
 };
 constexpr int kMaxBlock = 512;
 
@@ -110,14 +110,13 @@ void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const 
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
 // tileCounter (two device words, zero between launches; NULL for one block
-// per tile of particles): the neighbour passes' persistent grid, whose
+// per tile of particles): the solver passes' persistent grid, whose
 // blocks take the tiles from it (LaunchShape::persistent).
 // algorithm: LaunchShape::friendsAlgorithm.  Every build writes the circle
 // rows into `list`; none writes the flat rows (the first density pass
 // records them), so the return value, whether `flat` was written, is false.
 bool launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, int* tileCounter,
-                          cudaStream_t s);
+                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s);
 // The flat rows from the circle rows, when no density pass records them.
 void launch_flatten_friends(const DevConsts& c, const uint32_t* list, const uint2* meta, uint32_t* flat, cudaStream_t s);
 // flatIn / flatOut (may be NULL): the friends recorded in order as flat rows

@@ -262,15 +262,12 @@ __device__ __forceinline__ void friends_scan_global(const DevConsts& c, uint32_t
 template <int U, bool Narrow>
 __global__ void __launch_bounds__(kMaxBlock)
 build_friends_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, const uint2* __restrict__ cells,
-                     uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err, int tiles,
-                     int* tileCounter) {
-    for_tiles(tiles, tileCounter, [&](int tile) {
-        const int i = tile * (int)blockDim.x + (int)threadIdx.x;
-        if (i >= c.n) return;
-        FriendCircles<Narrow> fc(c, list, i, pred[i]);
-        friends_scan_global<U>(c, key_base(b, i), pred, cells, err, fc);
-        fc.finish(meta);
-    });
+                     uint32_t* __restrict__ list, uint2* __restrict__ meta, int* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n) return;
+    FriendCircles<Narrow> fc(c, list, i, pred[i]);
+    friends_scan_global<U>(c, key_base(b, i), pred, cells, err, fc);
+    fc.finish(meta);
 }
 
 // The same lists with the candidates streamed through shared memory, one
@@ -1050,8 +1047,7 @@ unsigned grid_for_tiles(K kernel, int n, int block, bool persistent, int* tiles)
 }
 
 bool launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const uint32_t* cells, uint32_t* list,
-                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, int* tileCounter,
-                          cudaStream_t s) {
+                          uint32_t* flat, uint2* meta, int* errorWord, int block, int algorithm, cudaStream_t s) {
     const bool pow2 = (c.grid & (c.grid - 1)) == 0;
     const uint32_t keys = c.grid * (uint32_t)(b.scenes ? b.nscenes : 1);
     const uint2* cellPairs = reinterpret_cast<const uint2*>(cells);
@@ -1066,10 +1062,10 @@ bool launch_build_friends(const DevConsts& c, Batch b, const float4* pred, const
         build_friends_warp_kernel<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, cellPairs, list, meta, errorWord);
         return false;
     }
+    // one block per tile: the tile loop of a persistent grid costs this kernel
+    // spilled registers in its candidate loop, and the grid gains nothing
     auto k = narrow ? build_friends_kernel<2, true> : build_friends_kernel<2, false>;
-    int tiles = 0;
-    const unsigned grid = grid_for_tiles(k, c.n, block, tileCounter != nullptr, &tiles);
-    k<<<grid, block, 0, s>>>(c, b, pred, cellPairs, list, meta, errorWord, tiles, tileCounter);
+    k<<<blocks_for(c.n, block), block, 0, s>>>(c, b, pred, cellPairs, list, meta, errorWord);
     return false;
 }
 
