@@ -622,7 +622,7 @@ __device__ __forceinline__ void compute_scaling_body(const DevConsts& c, const f
     const uint64_t mt = load_meta(meta, i);
     // complete neighbour sets count the particle itself first: d = h^2 - 0
     float ds = c.complete ? c.h2 * c.h2 * c.h2 : 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
-    constexpr int U = W != kWalkRows && !R ? 2 : 4;  // friends in flight: exact passes are register-bound, relaxed ones latency-bound
+    constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
     gather_walk<W, U>(list, flatIn, flatOut, n, i, FriendRows(mt, kept_density(mt), c.perCircle),
                       [&](uint32_t j) { return __ldg(pred + checked_index(j, (uint32_t)n, c.err, kErrFriendIndex)); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -704,7 +704,7 @@ __device__ __forceinline__ void compute_delta_body(const DevConsts& c, const Bat
     const float4 pi = pp[i];
     const uint64_t mt = load_meta(meta, i);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    constexpr int U = W != kWalkRows && !R ? 2 : 4;  // friends in flight: exact passes are register-bound, relaxed ones latency-bound
+    constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
     gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
                       [&](uint32_t j) { return __ldg(pp + checked_index(j, (uint32_t)n, c.err, kErrFriendIndex)); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -836,7 +836,7 @@ __device__ __forceinline__ void apply_viscosity_body(const DevConsts& c, const B
     const float4 pi = pred[i], vi = velIn[i];
     const uint64_t mt = load_meta(meta, i);
     float vsx = 0.0f, vsy = 0.0f, vsz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
-    constexpr int U = W != kWalkRows && !R ? 2 : 4;  // friends in flight: exact passes are register-bound, relaxed ones latency-bound
+    constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
     gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
                       [&](uint32_t j) { j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex); return PairRec{__ldg(pred + j), __ldg(velIn + j)}; }, [&](const PairRec& q) {
         const float4 pj = q.a;
@@ -916,7 +916,7 @@ __device__ __forceinline__ void apply_vorticity_body(const DevConsts& c, const f
     const float4 pi = pred[i];
     const uint64_t mt = load_meta(meta, i);
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    constexpr int U = W != kWalkRows && !R ? 2 : 4;  // friends in flight: exact passes are register-bound, relaxed ones latency-bound
+    constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
     gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
                       [&](uint32_t j) { j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex); return PairRec{__ldg(pred + j), __ldg(omega + j)}; }, [&](const PairRec& q) {
         const float4 pj = q.a;
