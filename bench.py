@@ -430,7 +430,8 @@ def batched_block(args, single_value: float, device_index: int) -> dict:
     sub, iters = int(scenes[0].subSteps), int(scenes[0].simIterations)
     sim = pbf.Simulation.create(scenes, pos, np.zeros_like(pos), device=device_index)
     stream = torch.cuda.ExternalStream(sim.stream(), device=torch.device("cuda", device_index))
-    for _ in range(args.batch_warmup):
+    warmup = args.batch_warmup if args.batch_warmup >= 0 else args.warmup  # as many frames as the single scene
+    for _ in range(warmup):
         sim.step_async(sub)
     sim.synchronize()
     blocks = sim.autotune(trial_substeps=2)
@@ -449,6 +450,7 @@ def batched_block(args, single_value: float, device_index: int) -> dict:
     launches0 = sim.launch_count()
     ms, clocks = timed_frames(sim, stream, args.batch_steps, sub, device_index)
     launches = sim.launch_count() - launches0
+    stage_ms, bnl, bnd, _, _ = replay_stages(sim, start_pos, start_vel, args.batch_steps, sub)
     sim.close()
     rate = total * iters * sub / (ms / 1e3)
     seq_ms = 0.0
@@ -471,7 +473,9 @@ def batched_block(args, single_value: float, device_index: int) -> dict:
                         f"(seed 7), box fill 0.3, gravity tilted U(0, 10) deg, XSPH c U(0.005, 0.05); {iters} "
                         f"iterations x {sub} substeps per frame, one CUDA graph per substep",
             "particles": total, "value": rate, "unit": UNIT, "ms_per_step": ms, "steps": args.batch_steps,
-            "warmup": args.batch_warmup, "gpu_launches": int(launches),
+            "warmup": warmup, "gpu_launches": int(launches),
+            "stage_ms_per_step": {k: round(v, 4) for k, v in sorted(stage_ms.items(), key=lambda kv: -kv[1])},
+            "neighbours": {"density_pass": bnl, "other_passes": bnd},
             "ratio_vs_single_scene": rate / single_value, "single_scene_value": single_value,
             "sequential_value": seq_rate, "ratio_vs_sequential": rate / seq_rate,
             "sequential_steps": args.batch_seq_steps,
@@ -922,7 +926,8 @@ def main() -> None:
     ap.add_argument("--no-batched", action="store_true", help="leave the batched block out of the default run")
     ap.add_argument("--batch-scenes", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=10, help="timed frames of the batch")
-    ap.add_argument("--batch-warmup", type=int, default=20, help="warm-up frames of the batch")
+    ap.add_argument("--batch-warmup", type=int, default=-1,
+                    help="warm-up frames of the batch (default: --warmup, as the single scene)")
     ap.add_argument("--batch-seq-steps", type=int, default=5, help="timed frames of each scene run alone")
     ap.add_argument("--rollout", action="store_true", help="differentiable rollout forward/backward alone")
     ap.add_argument("--no-rollout", action="store_true", help="leave the rollout block out of the default run")
