@@ -92,16 +92,16 @@ STAGE_BYTES = {
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and warp
 # instructions (smsp__inst_executed.sum) per launch, the mean over the four
 # launches of each pass in one substep (for the density pass: the one that
-# records the flat friend rows and three that read them), from ncu captures of
-# the dam_break_1m scene in the first substep of frame 51 (256-thread blocks,
-# plain thread map), with the mean list lengths of that substep (density pass
-# nl, other passes nd).  Scaled to the measured list lengths: the traffic by
-# the stage's list-inclusive bytes, the instructions in proportion to the
-# list length of the pass.
-TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 311.79e6, "nl": 38.88, "nd": 33.07},
-                   "computeDelta": {"bytes": 219.73e6, "nl": 38.88, "nd": 33.07}}
-ISSUE_CAPTURE = {"computeScaling": {"inst": 152.28e6, "nl": 38.88, "nd": 33.07},
-                 "computeDelta": {"inst": 148.34e6, "nl": 38.88, "nd": 33.07}}
+# records the flat friend rows and three that read them), from an ncu capture
+# of the dam_break_1m scene in the first substep of frame 51 (128-thread
+# blocks, balanced thread map), with the mean list lengths of that frame
+# (density pass nl, other passes nd).  Scaled to the measured list lengths:
+# the traffic by the stage's list-inclusive bytes, the instructions in
+# proportion to the list length of the pass.
+TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 314.85e6, "nl": 38.52, "nd": 32.79},
+                   "computeDelta": {"bytes": 219.98e6, "nl": 38.52, "nd": 32.79}}
+ISSUE_CAPTURE = {"computeScaling": {"inst": 138.53e6, "nl": 38.52, "nd": 32.79},
+                 "computeDelta": {"inst": 125.25e6, "nl": 38.52, "nd": 32.79}}
 SM_COUNT = 152
 SCHEDULERS_PER_SM = 4
 
@@ -659,8 +659,8 @@ def gpu_arm(args) -> None:
         issue = {"kernel": dominant, "warp_instructions_per_launch": inst,
                  "achieved": inst / (launch_ms / 1000.0), "peak": peak_issue, "unit": "warp instructions/s",
                  "frac": inst / (launch_ms / 1000.0) / peak_issue,
-                 "source": "ncu smsp__inst_executed.sum of one launch in the first substep of frame 51 (256-thread "
-                           "blocks, plain thread map, list length 38.88 / 33.07), scaled by list length"}
+                 "source": "ncu smsp__inst_executed.sum, mean launch of the pass in the first substep of frame 51 "
+                           "(128-thread blocks, balanced thread map, list length 38.52 / 32.79), scaled by list length"}
 
     # ---- the other arithmetic mode, same start state, its own block sizes ----
     other_line = None
