@@ -66,7 +66,7 @@ def _run(cmd: list[str]) -> tuple[int, str]:
 
 
 def _headers() -> list[Path]:
-    return sorted(CSRC.glob("*.h")) + sorted((REPO / "include").glob("*.h"))
+    return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted((REPO / "include").glob("*.h"))
 
 
 def _stale(obj: Path, src: Path) -> bool:

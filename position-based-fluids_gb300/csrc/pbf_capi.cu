@@ -51,6 +51,9 @@ struct pbf_ctx {
     uint32_t* list = nullptr;
     uint32_t* flat = nullptr;    // the friends of the substep in order, one flat row per position (see enqueue_substep)
     uint2* meta = nullptr;       // per-particle friend counts per circle + kept circles
+    uint32_t* taint = nullptr;          // per particle: the substep that tainted it (pbf::DevConsts::taint)
+    int4* cellXYZ = nullptr;            // per particle: its cell at the friends build and the scene's first key
+    uint32_t* irregularList = nullptr;  // particles found at irregular positions (pbf::DevConsts::irregularList)
     int* errWord = nullptr;
     int* tileCounters = nullptr;  // 2 words per neighbour kernel: its persistent grid's tile counter
     size_t histWords = 0;
@@ -227,16 +230,18 @@ DevConsts make_consts(const PbfParameters& p, int n) {
     c.complete = p.completeNeighbours ? 1 : 0;
     c.dpScale = c.negGradSpiky / c.rho0;
     c.invPoly6q = 1.0f / c.poly6q;
-    // Exact-mode quotients by reciprocal (quotient_rn in pbf_device.cuh).  With
-    // every coordinate 0 or at least 2^-37 in magnitude, a coordinate
-    // difference is 0 or at least 2^-60, and |r| (when r != 0) is normal.  A
-    // nonzero remaining distance h - |r| is at least h 2^-25 (one half ulp of
-    // h), so the density pass's numerator gradSpiky (h - |r|)^2 r_x is 0 or at
-    // least gradSpiky (h 2^-25)^2 2^-60, which must not fall below 2^-100; the
-    // quotients themselves are at most gradSpiky h^2 (|r_x| <= |r|).
+    // Exact-mode quotients by reciprocal (quotient_rn in pbf_device.cuh).  For
+    // particles whose friends all sit at coordinates that are 0 or at least
+    // 2^-27 in magnitude (the others divide the IEEE way), a coordinate
+    // difference is 0 or at least 2^-50, so r^2 is 0 or at least 2^-100 and
+    // |r| (when r != 0) is normal.  A nonzero remaining distance h - |r| is at
+    // least h 2^-25 (one half ulp of h), so the density pass's numerator
+    // gradSpiky (h - |r|)^2 r_x is 0 or at least gradSpiky (h 2^-25)^2 2^-50,
+    // which must not fall below 2^-100; the quotients themselves are at most
+    // gradSpiky h^2 (|r_x| <= |r|).
     const double hrMin = (double)p.h * std::ldexp(1.0, -25);
     c.quotients = (p.h >= std::ldexp(1.0f, -10) && p.h <= 1024.0f &&
-                   (double)c.gradSpiky * hrMin * hrMin >= std::ldexp(1.0, -40) &&
+                   (double)c.gradSpiky * hrMin * hrMin >= std::ldexp(1.0, -50) &&
                    (double)c.gradSpiky * (double)p.h * (double)p.h < 1e30) ? 1 : 0;
     // s_corr: for r^2 < h^2 the numerator (h^2 - r^2)^3 is at least
     // (h^2 2^-25)^3 >= 2^-99 when h^2 >= 2^-8, and with poly6q <= h^6 <= 1 the
@@ -325,7 +330,12 @@ void apply_planes(pbf_ctx* ctx) {
     ctx->consts.maskH = ctx->maskH;
     ctx->consts.wave = ctx->waveDev;
     ctx->consts.err = ctx->errWord;
-    ctx->consts.irregular = ctx->errWord + 1;
+    ctx->consts.epoch = reinterpret_cast<uint32_t*>(ctx->errWord + 1);
+    ctx->consts.irregularCount = reinterpret_cast<uint32_t*>(ctx->errWord + 2);
+    ctx->consts.taint = ctx->taint;
+    ctx->consts.cellXYZ = ctx->cellXYZ;
+    // the record of irregular positions: exact mode (relaxed passes divide no way but their own)
+    ctx->consts.irregularList = ctx->consts.relaxed ? nullptr : ctx->irregularList;
 }
 
 // The captured substep; the reverse pass's segment graphs are dropped with
@@ -473,10 +483,11 @@ __global__ void pack_density_kernel(int n, float4* pred, const float* density) {
 // Enqueue one Simulation::Step on the context's stream; with a tape, also
 // copy out what the reverse pass needs.
 int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tape = nullptr) {
-    const pbf::DevConsts& c = ctx->consts;
+    const bool paused = ctx->paused != 0;
+    pbf::DevConsts c = ctx->consts;
+    if (paused) c.quotients = 0;  // no sort: the keys need not give the cells of the friends build
     cudaStream_t s = ctx->stream;
     const int P = ctx->curPos, V = ctx->curVel;
-    const bool paused = ctx->paused != 0;
     uint64_t launched = 0;
     bool rangeOpen = false;
     auto mark = [&](const char* name, int iteration = -1) {
@@ -530,6 +541,13 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     // recorded by the first density pass (or flattened when there is none)
     bool haveFlat = pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, flat, meta, ctx->errWord,
                                               ls.friends, ls.friendsAlgorithm, s);
+    // the particles next to irregular positions divide the IEEE way (pbf::quotients_tainted)
+    auto taint = [&]() {
+        if (!c.irregularList) return;
+        pbf::launch_taint_neighbours(c, keys, s);
+        ++launched;
+    };
+    taint();
     mark("resetPartList");
     pbf::launch_reset_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s);
     launched += 3;
@@ -547,6 +565,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
                                   it + 1 == iters, tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr,
                                   flat, ls.delta, ls.balance, tiles(2), s);
         launched += 2;
+        taint();
     }
     if (!haveFlat) {
         pbf::launch_flatten_friends(c, list, meta, flat, s);
@@ -860,9 +879,10 @@ int pbf_create(const PbfParameters* params, int device, pbf_ctx** out) {
     ctx->device = device;
     PBF_CUDA(nullptr, cudaSetDevice(device));
     PBF_CUDA(nullptr, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-    // [0]: the error word; [1]: the sticky "irregular coordinate" flag of the exact quotients
-    PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->errWord, 2 * sizeof(int)));
-    PBF_CUDA(nullptr, cudaMemset(ctx->errWord, 0, 2 * sizeof(int)));
+    // [0]: the error word; [1]: the substep counter of the taint marks (pbf::DevConsts::epoch);
+    // [2]: the number of recorded irregular positions (pbf::DevConsts::irregularCount)
+    PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->errWord, 3 * sizeof(int)));
+    PBF_CUDA(nullptr, cudaMemset(ctx->errWord, 0, 3 * sizeof(int)));
     PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->tileCounters, 10 * sizeof(int)));
     PBF_CUDA(nullptr, cudaMemset(ctx->tileCounters, 0, 10 * sizeof(int)));
     *out = ctx.release();
@@ -880,6 +900,7 @@ int pbf_destroy(pbf_ctx* ctx) {
     }
     dev_free(ctx->omega); dev_free(ctx->density); dev_free(ctx->hist); dev_free(ctx->cells);
     dev_free(ctx->list); dev_free(ctx->flat); dev_free(ctx->meta); dev_free(ctx->errWord); dev_free(ctx->tileCounters);
+    dev_free(ctx->taint); dev_free(ctx->cellXYZ); dev_free(ctx->irregularList);
     dev_free(ctx->scenes); dev_free(ctx->sceneOf); dev_free(ctx->ids); dev_free(ctx->idsTmp);
     dev_free(ctx->quadsDev); dev_free(ctx->maskDev); dev_free(ctx->waveDev);
     if (ctx->timingAnchor) cudaEventDestroy(ctx->timingAnchor);
@@ -974,9 +995,15 @@ int pbf_init_cells(pbf_ctx* ctx) {
     ctx->cellsN = ctx->n;
     ++ctx->epoch;
     if ((rc = dev_alloc(ctx, &ctx->list, (size_t)ctx->listSlots * ctx->n)) ||
-        (rc = dev_alloc(ctx, &ctx->flat, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->meta, ctx->n)))
+        (rc = dev_alloc(ctx, &ctx->flat, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->meta, ctx->n)) ||
+        (rc = dev_alloc(ctx, &ctx->taint, ctx->n)) || (rc = dev_alloc(ctx, &ctx->cellXYZ, ctx->n)) ||
+        (rc = dev_alloc(ctx, &ctx->irregularList, ctx->n)))
         return rc;
     PBF_CUDA(ctx, cudaMemset(ctx->meta, 0, 8 * (size_t)ctx->n));
+    // taint marks are substep numbers from 1 on (the counter restarts with them); no record pending
+    PBF_CUDA(ctx, cudaMemset(ctx->taint, 0, 4 * (size_t)ctx->n));
+    PBF_CUDA(ctx, cudaMemset(ctx->errWord + 1, 0, 2 * sizeof(int)));
+    apply_planes(ctx);
     ctx->cellsReady = true;
     ctx->kernelsReady = false;
     return PBF_OK;
@@ -1375,8 +1402,6 @@ int pbf_write_state_async(pbf_ctx* ctx, const float* pos, const float* vel) {
     const size_t bytes = 16 * (size_t)ctx->n;
     if (pos) {
         PBF_CUDA(ctx, cudaMemcpyAsync(ctx->pos[ctx->curPos], pos, bytes, cudaMemcpyHostToDevice, ctx->stream));
-        // new positions: the irregular-coordinate flag starts over (predict checks every prediction)
-        PBF_CUDA(ctx, cudaMemsetAsync(ctx->errWord + 1, 0, sizeof(int), ctx->stream));
         // the written records become particles 0 .. N-1
         iota_kernel<<<(ctx->n + 255) / 256, 256, 0, ctx->stream>>>(ctx->n, ctx->ids);
         PBF_CUDA(ctx, cudaGetLastError());

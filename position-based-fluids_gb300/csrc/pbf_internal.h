@@ -47,12 +47,16 @@ struct DevConsts {
     // Exact passes: quotients by |r| and by poly6q through a correctly rounded
     // reciprocal and one remainder correction (quotient_rn), where the
     // parameters keep every numerator and quotient in the range that makes it
-    // equal to IEEE division (make_consts decides), and while no predicted
-    // coordinate is tiny and nonzero (*irregular stays 0; see note_irregular).
+    // equal to IEEE division (make_consts decides), for the particles whose
+    // friends all sit at regular positions (exact_quotients).
     int quotients;               // divisions by |r| in the four neighbour passes
     int quotientPoly6q;          // the s_corr division by poly6q in the position pass
     float recipPoly6q;           // RN(1 / poly6q)
-    int* irregular;              // device word, sticky: a predicted coordinate in (0, 2^-37) was written
+    uint32_t* epoch;             // device word: the substep's number, counted by the predict kernel
+    uint32_t* taint;             // per particle: the last substep that tainted it (quotients_tainted)
+    int4* cellXYZ;               // per particle: the cell its friends were taken around, and the scene's first key
+    uint32_t* irregularList;     // particles found at irregular positions by the last writing kernel
+    uint32_t* irregularCount;    // device word: their number (the taint kernel resets it)
     int circles, perCircle;
     uint32_t grid;
     int n;
@@ -108,6 +112,11 @@ void launch_compute_keys(const DevConsts& c, Batch b, const float4* pred, uint32
 void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, const uint32_t* ids,
                           float4* posOut, float4* predOut, uint32_t* idsOut, int* err, cudaStream_t s);
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
+// Taints, for the rest of the substep, every particle of the 27 cells around
+// each particle recorded at an irregular position since the last call
+// (DevConsts::irregularList), and empties the record.  keys: the substep's
+// sorted cell keys.
+void launch_taint_neighbours(const DevConsts& c, const uint32_t* keys, cudaStream_t s);
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
 // tileCounter (two device words, zero between launches; NULL for one block
 // per tile of particles): the solver passes' persistent grid, whose

@@ -71,7 +71,7 @@ __global__ void predict_keys_kernel(DevConsts c, Batch b, const float4* __restri
     const float4 p = pos[i];
     const float4 q = make_float4(p.x + c.dt * v.x, p.y + c.dt * v.y, p.z + c.dt * v.z, p.w + c.dt * v.w);
     pred[i] = q;
-    note_irregular(c.irregular, q.x, q.y, q.z);
+    if (i == 0) *c.epoch += 1u;  // a new substep: earlier taint marks lapse
     if (!paused) {
         keys[i] = base + grid_hash(__float2int_rz(q.x / c.h), __float2int_rz(q.y / c.h), __float2int_rz(q.z / c.h), c.grid);
         perm[i] = (uint32_t)i;
@@ -121,6 +121,45 @@ __global__ void update_cells_kernel(int n, const uint32_t* __restrict__ keys, ui
     } else {
         cells[2 * (size_t)k] = 0u;
     }
+}
+
+// The first index of the sorted keys at or above k, found by a whole warp:
+// each step probes 32 evenly spaced keys of the interval that holds the
+// answer and keeps the 1/32 of it between the last probe below k and the
+// next, so 2^20 keys take four dependent loads.
+__device__ __forceinline__ uint32_t warp_lower_bound(const uint32_t* __restrict__ keys, uint32_t n, uint32_t k,
+                                                     uint32_t lane) {
+    uint32_t lo = 0, hi = n;  // the answer lies in [lo, hi]
+    while (hi - lo > 32u) {
+        const uint32_t step = (hi - lo + 31u) / 32u;
+        const uint32_t probe = lo + lane * step;
+        const uint32_t below = __popc(__ballot_sync(0xFFFFFFFFu, probe < hi && keys[probe] < k));
+        if (below == 0u) return lo;
+        const uint32_t next = lo + below * step;
+        lo = lo + (below - 1u) * step + 1u;
+        hi = min(hi, next);
+    }
+    return lo + __popc(__ballot_sync(0xFFFFFFFFu, lo + lane < hi && keys[lo + lane] < k));
+}
+
+// Every particle of the 27 cells around each particle recorded at an
+// irregular position (DevConsts::irregularList), tainted for the rest of the
+// substep; a cell's particles are the run of its key in the sorted keys.  One
+// block of 32 warps, a warp per (recorded particle, cell), which then empties
+// the record for the next writer.
+constexpr int kTaintThreads = 1024;
+__global__ void __launch_bounds__(kTaintThreads) taint_neighbours_kernel(DevConsts c, const uint32_t* __restrict__ keys) {
+    const uint32_t count = *c.irregularCount, e = *c.epoch, n = (uint32_t)c.n;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (uint32_t pair = warp; pair < 27u * count; pair += kTaintThreads / 32) {
+        const int4 q = c.cellXYZ[c.irregularList[pair / 27u]];
+        const int k = (int)(pair % 27u);
+        const uint32_t key = (uint32_t)q.w + grid_hash(q.x + k / 9 - 1, q.y + (k / 3) % 3 - 1, q.z + k % 3 - 1, c.grid);
+        const uint32_t first = warp_lower_bound(keys, n, key, lane), end = warp_lower_bound(keys, n, key + 1u, lane);
+        for (uint32_t p = first + lane; p < end; p += 32u) c.taint[p] = e;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *c.irregularCount = 0u;
 }
 
 // reset_grid.cl:6-14
@@ -224,6 +263,7 @@ __device__ __forceinline__ void friends_scan_global(const DevConsts& c, uint32_t
     const uint32_t eym = expand_bits(cy - 1) << 1, ey0 = expand_bits(cy) << 1, eyp = expand_bits(cy + 1) << 1;
     const uint32_t ezm = expand_bits(cz - 1) << 2, ez0 = expand_bits(cz) << 2, ezp = expand_bits(cz + 1) << 2;
     const uint32_t selfHash = pow2 ? ((ex0 | ey0 | ez0) & mask) : ((ex0 | ey0 | ez0) % c.grid);
+    record_cell(c, i, pi, cx, cy, cz, base);
     auto scan = [&](uint32_t lo, uint32_t hi) {
         uint32_t j = lo;
         for (; j + (U - 1) <= hi; j += U) {
@@ -373,6 +413,7 @@ build_friends_brick_kernel(DevConsts c, const float4* __restrict__ pred, const u
         const int cx = __float2int_rz(fc.pi.x / c.h), cy = __float2int_rz(fc.pi.y / c.h), cz = __float2int_rz(fc.pi.z / c.h);
         const int lx = cx - bx, ly = cy - by, lz = cz - bz;
         if (useSmem && (unsigned)lx < (unsigned)B && (unsigned)ly < (unsigned)B && (unsigned)lz < (unsigned)B) {
+            record_cell(c, i, fc.pi, cx, cy, cz, base);
             // staged entries [a, b) of one cell, candidates st + (k - off), two in flight, self skipped
             auto scanStaged = [&](uint32_t a, uint32_t b, uint32_t jOfA) {
                 uint32_t k = a;
@@ -428,6 +469,7 @@ build_friends_warp_kernel(DevConsts c, Batch b, const float4* __restrict__ pred,
     const int cx = __float2int_rz(pi.x / c.h), cy = __float2int_rz(pi.y / c.h), cz = __float2int_rz(pi.z / c.h);
     const uint32_t base = valid ? key_base(b, i) : 0u;
     const int C = c.circles, P = c.perCircle;
+    if (valid) record_cell(c, i, pi, cx, cy, cz, base);
     const bool pow2 = (c.grid & (c.grid - 1)) == 0;
     const uint32_t gmask = c.grid - 1;
     const int ux = __shfl_up_sync(kFull, cx, 1), uy = __shfl_up_sync(kFull, cy, 1), uz = __shfl_up_sync(kFull, cz, 1);
@@ -614,12 +656,8 @@ __device__ __forceinline__ void compute_scaling_body(const DevConsts& c, const f
                                                      float4* __restrict__ predPacked, float* __restrict__ density,
                                                      const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
                                                      const uint32_t* __restrict__ flatIn, uint32_t* __restrict__ flatOut,
-                                                     int tile) {
+                                                     int i, const float4 pi, uint64_t mt) {
     const int n = c.n;
-    const int i = B ? balanced_particle(meta, n, true, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
-    if (i < 0 || i >= n) return;
-    const float4 pi = pred[i];
-    const uint64_t mt = load_meta(meta, i);
     // complete neighbour sets count the particle itself first: d = h^2 - 0
     float ds = c.complete ? c.h2 * c.h2 * c.h2 : 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
     constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
@@ -642,12 +680,13 @@ __device__ __forceinline__ void compute_scaling_body(const DevConsts& c, const f
         } else {
             const float r2 = dot3(rx, ry, rz, rx, ry, rz);
             if (in_support(c, r2)) {
-                const float rl = sqrtf(r2);
+                float rl, y;
+                if (Q) sqrt_recip_rn(r2, rl, y);
+                else rl = sqrtf(r2);
                 const float hr = c.h - rl;
                 const float sc = c.gradSpiky * hr * hr;
                 float g0, g1, g2;
                 if (Q) {
-                    const float y = __frcp_rn(rl);
                     g0 = quotient_rn(sc * rx, rl, y);
                     g1 = quotient_rn(sc * ry, rl, y);
                     g2 = quotient_rn(sc * rz, rl, y);
@@ -679,10 +718,14 @@ compute_scaling_kernel(DevConsts c, const float4* __restrict__ pred, float4* __r
                        float* __restrict__ density, const uint32_t* __restrict__ list,
                        const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn,
                        uint32_t* __restrict__ flatOut, int tiles, int* tileCounter) {
-    const bool q = !R && exact_quotients(c);
     for_tiles(tiles, tileCounter, [&](int tile) {
-        if (q) compute_scaling_body<R, B, W, true>(c, pred, predPacked, density, list, meta, flatIn, flatOut, tile);
-        else compute_scaling_body<R, B, W, false>(c, pred, predPacked, density, list, meta, flatIn, flatOut, tile);
+        const int i = B ? balanced_particle(meta, c.n, true, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
+        if (i < 0 || i >= c.n) return;
+        const float4 pi = pred[i];
+        const uint64_t mt = load_meta(meta, i);
+        // a particle that may hold a friend at an irregular position divides the IEEE way
+        if (!R && c.quotients && !quotients_tainted(c, i)) compute_scaling_body<R, B, W, true>(c, pred, predPacked, density, list, meta, flatIn, flatOut, i, pi, mt);
+        else compute_scaling_body<R, B, W, false>(c, pred, predPacked, density, list, meta, flatIn, flatOut, i, pi, mt);
     });
 }
 
@@ -697,12 +740,8 @@ __device__ __forceinline__ void compute_delta_body(const DevConsts& c, const Bat
                                                    const float* __restrict__ density, const uint32_t* __restrict__ list,
                                                    const uint2* __restrict__ meta, int lastIteration,
                                                    uint8_t* __restrict__ clampMask, const uint32_t* __restrict__ flatIn,
-                                                   int tile) {
+                                                   int i, const float4 pi, uint64_t mt) {
     const int n = c.n;
-    const int i = B ? balanced_particle(meta, n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
-    if (i < 0 || i >= n) return;
-    const float4 pi = pp[i];
-    const uint64_t mt = load_meta(meta, i);
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
     gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
@@ -724,11 +763,12 @@ __device__ __forceinline__ void compute_delta_body(const DevConsts& c, const Bat
         } else {
             const float r2 = dot3(rx, ry, rz, rx, ry, rz);
             if (in_support(c, r2)) {
-                const float rl = sqrtf(r2);
+                float rl, y;
+                if (Q) sqrt_recip_rn(r2, rl, y);
+                else rl = sqrtf(r2);
                 const float hr = c.h - rl;
                 float g0, g1, g2;
                 if (Q) {
-                    const float y = __frcp_rn(rl);
                     g0 = quotient_rn(rx, rl, y) * hr * hr;
                     g1 = quotient_rn(ry, rl, y) * hr * hr;
                     g2 = quotient_rn(rz, rl, y) * hr * hr;
@@ -785,7 +825,7 @@ __device__ __forceinline__ void compute_delta_body(const DevConsts& c, const Bat
     const float dx = fx - pi.x, dy = fy - pi.y, dz = fz - pi.z;
     const float4 out = make_float4(pi.x + dx, pi.y + dy, pi.z + dz, lastIteration ? density[i] : pi.w + 0.0f);
     predOut[i] = out;
-    note_irregular(c.irregular, out.x, out.y, out.z);
+    if (!R) note_position(c, i, out.x, out.y, out.z);
 }
 
 template <bool R, bool B, int W>
@@ -794,10 +834,14 @@ compute_delta_kernel(DevConsts c, Batch b, const float4* __restrict__ pp, const 
                      float4* __restrict__ predOut, const float* __restrict__ density, const uint32_t* __restrict__ list,
                      const uint2* __restrict__ meta, int lastIteration, uint8_t* __restrict__ clampMask,
                      const uint32_t* __restrict__ flatIn, int tiles, int* tileCounter) {
-    const bool q = !R && exact_quotients(c);
     for_tiles(tiles, tileCounter, [&](int tile) {
-        if (q) compute_delta_body<R, B, W, true>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn, tile);
-        else compute_delta_body<R, B, W, false>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn, tile);
+        const int i = B ? balanced_particle(meta, c.n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
+        if (i < 0 || i >= c.n) return;
+        const float4 pi = pp[i];
+        const uint64_t mt = load_meta(meta, i);
+        // a particle that may hold a friend at an irregular position divides the IEEE way
+        if (!R && c.quotients && !quotients_tainted(c, i)) compute_delta_body<R, B, W, true>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn, i, pi, mt);
+        else compute_delta_body<R, B, W, false>(c, b, pp, posPrev, predOut, density, list, meta, lastIteration, clampMask, flatIn, i, pi, mt);
     });
 }
 
@@ -829,12 +873,8 @@ __device__ __forceinline__ void apply_viscosity_body(const DevConsts& c, const B
                                                      const float4* __restrict__ velIn, float4* __restrict__ velOut,
                                                      float4* __restrict__ omega, const uint32_t* __restrict__ list,
                                                      const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn,
-                                                     int tile) {
+                                                     int i, const float4 pi, const float4 vi, uint64_t mt) {
     const int n = c.n;
-    const int i = B ? balanced_particle(meta, n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
-    if (i < 0 || i >= n) return;
-    const float4 pi = pred[i], vi = velIn[i];
-    const uint64_t mt = load_meta(meta, i);
     float vsx = 0.0f, vsy = 0.0f, vsz = 0.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
     constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
     gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
@@ -858,11 +898,12 @@ __device__ __forceinline__ void apply_viscosity_body(const DevConsts& c, const B
                 vsy = fmaf(uy, d3, vsy);
                 vsz = fmaf(uz, d3, vsz);
             } else {
-                const float rl = sqrtf(r2);
+                float rl, y;
+                if (Q) sqrt_recip_rn(r2, rl, y);
+                else rl = sqrtf(r2);
                 const float hr = c.h - rl;
                 float g0, g1, g2;
                 if (Q) {
-                    const float y = __frcp_rn(rl);
                     g0 = quotient_rn(rx, rl, y) * hr * hr;
                     g1 = quotient_rn(ry, rl, y) * hr * hr;
                     g2 = quotient_rn(rz, rl, y) * hr * hr;
@@ -896,10 +937,14 @@ apply_viscosity_kernel(DevConsts c, Batch b, const float4* __restrict__ pred, co
                        float4* __restrict__ velOut, float4* __restrict__ omega,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
                        const uint32_t* __restrict__ flatIn, int tiles, int* tileCounter) {
-    const bool q = !R && exact_quotients(c);
     for_tiles(tiles, tileCounter, [&](int tile) {
-        if (q) apply_viscosity_body<R, B, W, true>(c, b, pred, velIn, velOut, omega, list, meta, flatIn, tile);
-        else apply_viscosity_body<R, B, W, false>(c, b, pred, velIn, velOut, omega, list, meta, flatIn, tile);
+        const int i = B ? balanced_particle(meta, c.n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
+        if (i < 0 || i >= c.n) return;
+        const float4 pi = pred[i], vi = velIn[i];
+        const uint64_t mt = load_meta(meta, i);
+        // a particle that may hold a friend at an irregular position divides the IEEE way
+        if (!R && c.quotients && !quotients_tainted(c, i)) apply_viscosity_body<R, B, W, true>(c, b, pred, velIn, velOut, omega, list, meta, flatIn, i, pi, vi, mt);
+        else apply_viscosity_body<R, B, W, false>(c, b, pred, velIn, velOut, omega, list, meta, flatIn, i, pi, vi, mt);
     });
 }
 
@@ -909,12 +954,8 @@ __device__ __forceinline__ void apply_vorticity_body(const DevConsts& c, const f
                                                      const float4* __restrict__ omega, const float4* __restrict__ velIn,
                                                      float4* __restrict__ velOut, const uint32_t* __restrict__ list,
                                                      const uint2* __restrict__ meta, const uint32_t* __restrict__ flatIn,
-                                                     int tile) {
+                                                     int i, const float4 pi, uint64_t mt) {
     const int n = c.n;
-    const int i = B ? balanced_particle(meta, n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
-    if (i < 0 || i >= n) return;
-    const float4 pi = pred[i];
-    const uint64_t mt = load_meta(meta, i);
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
     constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
     gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
@@ -933,11 +974,12 @@ __device__ __forceinline__ void apply_vorticity_body(const DevConsts& c, const f
                 ey = fmaf(s, ry, ey);
                 ez = fmaf(s, rz, ez);
             } else {
-                const float rl = sqrtf(r2);
+                float rl, y;
+                if (Q) sqrt_recip_rn(r2, rl, y);
+                else rl = sqrtf(r2);
                 const float hr = c.h - rl;
                 float g0, g1, g2;
                 if (Q) {
-                    const float y = __frcp_rn(rl);
                     g0 = quotient_rn(rx, rl, y) * hr * hr;
                     g1 = quotient_rn(ry, rl, y) * hr * hr;
                     g2 = quotient_rn(rz, rl, y) * hr * hr;
@@ -986,10 +1028,14 @@ apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float
                        const float4* __restrict__ velIn, float4* __restrict__ velOut,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
                        const uint32_t* __restrict__ flatIn, int tiles, int* tileCounter) {
-    const bool q = !R && exact_quotients(c);
     for_tiles(tiles, tileCounter, [&](int tile) {
-        if (q) apply_vorticity_body<R, B, W, true>(c, pred, omega, velIn, velOut, list, meta, flatIn, tile);
-        else apply_vorticity_body<R, B, W, false>(c, pred, omega, velIn, velOut, list, meta, flatIn, tile);
+        const int i = B ? balanced_particle(meta, c.n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
+        if (i < 0 || i >= c.n) return;
+        const float4 pi = pred[i];
+        const uint64_t mt = load_meta(meta, i);
+        // a particle that may hold a friend at an irregular position divides the IEEE way
+        if (!R && c.quotients && !quotients_tainted(c, i)) apply_vorticity_body<R, B, W, true>(c, pred, omega, velIn, velOut, list, meta, flatIn, i, pi, mt);
+        else apply_vorticity_body<R, B, W, false>(c, pred, omega, velIn, velOut, list, meta, flatIn, i, pi, mt);
     });
 }
 
@@ -1009,6 +1055,10 @@ void launch_compute_keys(const DevConsts& c, Batch b, const float4* pred, uint32
 void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, const uint32_t* ids,
                           float4* posOut, float4* predOut, uint32_t* idsOut, int* err, cudaStream_t s) {
     gather_sorted_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, perm, pos, pred, ids, posOut, predOut, idsOut, err);
+}
+
+void launch_taint_neighbours(const DevConsts& c, const uint32_t* keys, cudaStream_t s) {
+    taint_neighbours_kernel<<<1, kTaintThreads, 0, s>>>(c, keys);
 }
 
 void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s) {

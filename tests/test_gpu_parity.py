@@ -184,14 +184,14 @@ def test_substeps_bit_exact(name, algorithm, pbf_mod, oracle_mod, cuda_device):
 
 
 def test_tiny_coordinates_bit_exact(pbf_mod, oracle_mod, cuda_device):
-    """Predicted coordinates in (0, 2^-37): their differences can be too small
-    for the exact passes' quotients through one reciprocal, so the library
-    notices them as predict writes them and divides the IEEE way from then
-    on.  A block at the origin (no clamp) with some particles moved onto tiny
-    coordinates next to neighbours at exactly 0."""
+    """Predicted coordinates in (0, 2^-27): their differences can be too small
+    for the exact passes' quotients through one reciprocal, so the particles
+    that may hold such a friend (the 27 cells around it) divide the IEEE way
+    for the rest of the substep.  A block at the origin (no clamp) with some
+    particles moved onto tiny coordinates next to neighbours at exactly 0."""
     params, pos, vel = scene(pbf_mod, (10, 10, 10), origin=(0.0, 0.0, 0.0), jitter=0.0, boxClamp=0)
     pos[1, 0] = np.float32(3e-13)       # x next to particle 0 at x = 0
-    pos[10, 1] = np.float32(1e-30)      # y, a normal float far below 2^-37
+    pos[10, 1] = np.float32(1e-30)      # y, a normal float far below 2^-27
     pos[100, 2] = np.float32(2e-42)     # z, subnormal
     pos[111, :3] = np.float32(5e-39)
     gp, gv, gpr, gcounts, glist = run_gpu(pbf_mod, params, pos, vel, 3, cuda_device)
@@ -200,6 +200,29 @@ def test_tiny_coordinates_bit_exact(pbf_mod, oracle_mod, cuda_device):
     assert_same("pos", gp, op)
     assert_same("vel", gv, ov)
     assert_same("pred", gpr, opr)
+
+
+def test_tiny_coordinates_arising_in_a_dam_break_bit_exact(pbf_mod, oracle_mod, cuda_device):
+    """Coordinates in (0, 2^-27) also arise by themselves: particles resting a
+    hair's breadth off a wall.  In the 65,536-particle double dam break with
+    4 iterations they appear from about substep 150 on, the oracle's states
+    show them, and the GPU's state equals the oracle's every 32 substeps
+    through substep 224."""
+    params, pos, vel = pbf_mod.make_double_dam_break(65536, iterations=4)
+    tiny = 0
+    p, v = pos, vel
+    with pbf_mod.Simulation.create(params, pos, vel, device=cuda_device) as sim:
+        for chunk in range(7):
+            for _ in range(32):
+                p, v, q = oracle_mod.step(params, p, v, 1)
+                x = np.abs(np.concatenate([p[:, :3], q[:, :3]]))
+                tiny += int(((x > 0) & (x < 2.0 ** -27)).sum())
+            sim.Step(32)
+            gp, gv, gq = sim.read_state()
+            assert_same(f"pos after {32 * (chunk + 1)} substeps", gp, p)
+            assert_same(f"vel after {32 * (chunk + 1)} substeps", gv, v)
+            assert_same(f"pred after {32 * (chunk + 1)} substeps", gq, q)
+    assert tiny > 0, "no coordinate in (0, 2^-27) arose: the case no longer covers them"
 
 
 def test_persistent_grids_bit_identical(pbf_mod, cuda_device):
