@@ -90,18 +90,24 @@ STAGE_BYTES = {
 }
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and warp
-# instructions (smsp__inst_executed.sum) per launch, the mean over the four
-# launches of each pass in one substep (for the density pass: the one that
-# records the flat friend rows and three that read them), from an ncu capture
-# of the dam_break_1m scene in the first substep of frame 51 (128-thread
-# blocks, balanced thread map), with the mean list lengths of that frame
-# (density pass nl, other passes nd).  Scaled to the measured list lengths:
-# the traffic by the stage's list-inclusive bytes, the instructions in
-# proportion to the list length of the pass.
-TRAFFIC_CAPTURE = {"computeScaling": {"bytes": 314.85e6, "nl": 38.52, "nd": 32.79},
-                   "computeDelta": {"bytes": 219.98e6, "nl": 38.52, "nd": 32.79}}
-ISSUE_CAPTURE = {"computeScaling": {"inst": 138.53e6, "nl": 38.52, "nd": 32.79},
-                 "computeDelta": {"inst": 125.25e6, "nl": 38.52, "nd": 32.79}}
+# instructions (smsp__inst_executed.sum) per launch from an ncu capture of the
+# dam_break_1m scene in the first substep of frame 51, with the mean list
+# lengths of that frame (density pass nl, other passes nd): the friends build,
+# and the mean over the four launches of each solver pass in the substep (for
+# the density pass: the one that records the flat friend rows and three that
+# read them).  Launch shape of the capture: the autotuner's for that state
+# (friends 128-thread blocks, solver passes 64, plain thread map).  Scaled to
+# the measured list lengths: the traffic by the stage's list-inclusive bytes,
+# the instructions in proportion to the list length of the pass (for the
+# friends build, whose candidates grow with the density, to nl).
+CAPTURE_SOURCE = ("ncu capture of the first substep of frame 51 (friends 128-thread blocks, solver passes 64, "
+                  "list lengths 38.52 / 32.79), scaled by list length")
+TRAFFIC_CAPTURE = {"buildFriendsList": {"bytes": 811.0e6, "nl": 38.52, "nd": 32.79},
+                   "computeScaling": {"bytes": 317.3e6, "nl": 38.52, "nd": 32.79},
+                   "computeDelta": {"bytes": 224.6e6, "nl": 38.52, "nd": 32.79}}
+ISSUE_CAPTURE = {"buildFriendsList": {"inst": 650.0e6, "nl": 38.52, "nd": 32.79},
+                 "computeScaling": {"inst": 115.0e6, "nl": 38.52, "nd": 32.79},
+                 "computeDelta": {"inst": 114.9e6, "nl": 38.52, "nd": 32.79}}
 SM_COUNT = 152
 SCHEDULERS_PER_SM = 4
 
@@ -651,16 +657,15 @@ def gpu_arm(args) -> None:
                      "note": "|rho / rho0 - 1| per particle, density of the last solver iteration"}
 
     issue = None
-    if dominant in ISSUE_CAPTURE and args.math == "exact":
+    if dominant in ISSUE_CAPTURE and (args.math == "exact" or dominant == "buildFriendsList"):
         cap = ISSUE_CAPTURE[dominant]
-        inst = cap["inst"] * (nl / cap["nl"] if dominant == "computeScaling" else nd / cap["nd"])
+        inst = cap["inst"] * (nl / cap["nl"] if dominant in ("computeScaling", "buildFriendsList") else nd / cap["nd"])
         clk = clocks.summary().get("sm_mhz") or 2070.0
         peak_issue = SM_COUNT * SCHEDULERS_PER_SM * clk * 1e6
         issue = {"kernel": dominant, "warp_instructions_per_launch": inst,
                  "achieved": inst / (launch_ms / 1000.0), "peak": peak_issue, "unit": "warp instructions/s",
                  "frac": inst / (launch_ms / 1000.0) / peak_issue,
-                 "source": "ncu smsp__inst_executed.sum, mean launch of the pass in the first substep of frame 51 "
-                           "(128-thread blocks, balanced thread map, list length 38.52 / 32.79), scaled by list length"}
+                 "source": "smsp__inst_executed.sum of the " + CAPTURE_SOURCE}
 
     # ---- the other arithmetic mode, same start state, its own block sizes ----
     other_line = None
