@@ -44,11 +44,11 @@ struct DevConsts {
     const float* wave;           // device scalar: the moving wall's offset from xMin (NULL: none)
     int* err;                    // the context's error word (bounds-checked builds record bad indices there)
     float dpScale, invPoly6q;    // -gradSpiky / rho0 and 1 / poly6q (relaxed variants only)
-    // Exact passes: quotients by |r| and by poly6q through a correctly rounded
-    // reciprocal and one remainder correction (quotient_rn), where the
+    // Exact passes: quotients by |r| and by poly6q through a reciprocal and
+    // one remainder correction (quotient_rn, sqrt_recip_rn), where the
     // parameters keep every numerator and quotient in the range that makes it
     // equal to IEEE division (make_consts decides), for the particles whose
-    // friends all sit at regular positions (exact_quotients).
+    // friends all sit at regular positions (quotients_tainted).
     int quotients;               // divisions by |r| in the four neighbour passes
     int quotientPoly6q;          // the s_corr division by poly6q in the position pass
     float recipPoly6q;           // RN(1 / poly6q)
