@@ -42,15 +42,23 @@ __device__ __forceinline__ float len(F3 a) { return sqrtf(dot(a, a)); }
 __device__ __forceinline__ void add3(float4* a, F3 v) { atomicAdd(a, make_float4(v.x, v.y, v.z, 0.0f)); }
 
 // k(r) and the adjoint of its argument: d/dr [k . kb] = f kb + f'(|r|)(kb.r) r/|r|
-// with f = (h-|r|)^2/|r|, f' = -(h-|r|)(h+|r|)/|r|^2.
-__device__ __forceinline__ F3 kvec(F3 r, float rl, float h) {
+// with f = (h-|r|)^2/|r|, f' = -(h-|r|)(h+|r|)/|r|^2.  y is 1/|r| within an
+// ulp (sqrt_recip_rn): the adjoint is an FP32 gradient, not a bit-exact one.
+__device__ __forceinline__ F3 kvec(F3 r, float rl, float y, float h) {
     const float hr = h - rl;
-    return (hr * hr / rl) * r;
+    return (hr * hr * y) * r;
 }
-__device__ __forceinline__ F3 kvec_adj(F3 r, float rl, float h, F3 kb) {
-    const float f = (h - rl) * (h - rl) / rl;
-    const float fp = -(h - rl) * (h + rl) / (rl * rl);
-    return f * kb + (fp * dot(kb, r) / rl) * r;
+__device__ __forceinline__ F3 kvec_adj(F3 r, float rl, float y, float h, F3 kb) {
+    const float hr = h - rl;
+    const float f = hr * hr * y;
+    const float fp = -hr * (h + rl) * y * y;
+    return f * kb + (fp * dot(kb, r) * y) * r;
+}
+// |r| and 1/|r| of a pair.
+__device__ __forceinline__ float pair_length(float r2, float& y) {
+    float rl;
+    sqrt_recip_rn(r2, rl, y);
+    return rl;
 }
 
 __device__ __forceinline__ bool xsph_pair(const DevConsts& c, float r2, float rhoj) {
@@ -87,7 +95,9 @@ adj_vorticity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
         const F3 r = pi - f3(pj);
         const float r2 = dot(r, r);
         if (!xsph_pair(c, r2, pj.w)) continue;
-        eta = eta + len(f3(omega[j])) * kvec(r, sqrtf(r2), c.h);
+        float y;
+        const float rl = pair_length(r2, y);
+        eta = eta + len(f3(omega[j])) * kvec(r, rl, y, c.h);
     }
     eta = -G * eta;
     const float l = len(eta);
@@ -99,21 +109,24 @@ adj_vorticity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
     add3(&omb[i], cross(ub, N));
     const F3 etab = (1.0f / l) * (Nb - dot(N, Nb) * N);
     FlatFriends f2(mt, kept_other(mt));
+    F3 pbi = {0.0f, 0.0f, 0.0f};  // particle i's own terms, added once
     for (int t = 0; t < f2.total; ++t) {
         const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const float4 pj = pI[j];
         const F3 r = pi - f3(pj);
         const float r2 = dot(r, r);
         if (!xsph_pair(c, r2, pj.w)) continue;
-        const float rl = sqrtf(r2);
-        const F3 k = kvec(r, rl, c.h);
+        float y;
+        const float rl = pair_length(r2, y);
+        const F3 k = kvec(r, rl, y, c.h);
         const F3 oj = f3(omega[j]);
         const float ol = len(oj);
         if (ol > 0.0f) add3(&omb[j], (-G * dot(etab, k) / ol) * oj);
-        const F3 rb = kvec_adj(r, rl, c.h, (-G * ol) * etab);
-        add3(&pb[i], rb);
+        const F3 rb = kvec_adj(r, rl, y, c.h, (-G * ol) * etab);
+        pbi = pbi + rb;
         add3(&pb[j], -1.0f * rb);
     }
+    add3(&pb[i], pbi);
 }
 
 // v3 = v2 + c POLY6 sum (v2_j - v2_i) W and omega = -G sum (v2_j - v2_i) x k:
@@ -130,7 +143,7 @@ adj_viscosity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
         const uint64_t mt = load_meta(meta, i);
         const F3 pi = f3(pI[i]), v3b = f3(vb[i]), ob = f3(omb[i]), vi = f3(v2[i]);
         const float G = c.gradSpiky;
-        add3(&v2b[i], v3b);
+        F3 v2bi = v3b, pbi = {0.0f, 0.0f, 0.0f};  // particle i's own terms, added once
         FlatFriends fr(mt, kept_other(mt));
         for (int t = 0; t < fr.total; ++t) {
             const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
@@ -138,20 +151,23 @@ adj_viscosity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
             const F3 r = pi - f3(pj);
             const float r2 = dot(r, r);
             if (!xsph_pair(c, r2, pj.w)) continue;
-            const float rl = sqrtf(r2);
+            float y;
+            const float rl = pair_length(r2, y);
             const F3 u = f3(v2[j]) - vi;
             const float d = c.h2 - r2;
             const float w = c.poly6 * d * d * d;
-            const F3 k = kvec(r, rl, c.h);
+            const F3 k = kvec(r, rl, y, c.h);
             cacc += w * dot(v3b, u);
             const F3 ub = (c.visc * w) * v3b + (-G) * cross(k, ob);
             add3(&v2b[j], ub);
-            add3(&v2b[i], -1.0f * ub);
+            v2bi = v2bi - ub;
             const float Wb = c.visc * c.poly6 * dot(v3b, u);
-            const F3 rb = (Wb * -6.0f * d * d) * r + kvec_adj(r, rl, c.h, (-G) * cross(ob, u));
-            add3(&pb[i], rb);
+            const F3 rb = (Wb * -6.0f * d * d) * r + kvec_adj(r, rl, y, c.h, (-G) * cross(ob, u));
+            pbi = pbi + rb;
             add3(&pb[j], -1.0f * rb);
         }
+        add3(&v2b[i], v2bi);
+        add3(&pb[i], pbi);
     }
     const float s = block_sum(cacc);
     if (threadIdx.x == 0 && s != 0.0f) atomicAdd(cbar, s);
@@ -184,7 +200,8 @@ adj_delta_kernel(DevConsts c, const float4* __restrict__ q, const uint8_t* __res
         if (m & 12) fb.y = 0.0f;
         if (m & 48) fb.z = 0.0f;
     }
-    add3(&pbt[i], fb);
+    F3 pbi = fb;  // particle i's own terms, added once
+    float lbi = 0.0f;
     const float4 qi = q[i];
     const F3 pi = f3(qi);
     const float a0 = -c.gradSpiky / c.rho0;
@@ -196,19 +213,22 @@ adj_delta_kernel(DevConsts c, const float4* __restrict__ q, const uint8_t* __res
         const F3 r = pi - f3(qj);
         const float r2 = dot(r, r);
         if (!in_support(c, r2)) continue;
-        const float rl = sqrtf(r2);
+        float y;
+        const float rl = pair_length(r2, y);
         const float d = c.h2 - r2;
         const float rq = d * d * d / c.poly6q;
         const float a = qi.w + qj.w + c.K * rq * rq * rq * rq;
-        const F3 k = kvec(r, rl, c.h);
+        const F3 k = kvec(r, rl, y, c.h);
         const float ab = a0 * dot(fb, k);
-        atomicAdd(&lb[i], ab);
+        lbi += ab;
         atomicAdd(&lb[j], ab);
         const float sW = ab * 4.0f * c.K * rq * rq * rq / c.poly6q;
-        const F3 rb = (sW * -6.0f * d * d) * r + kvec_adj(r, rl, c.h, (a0 * a) * fb);
-        add3(&pbt[i], rb);
+        const F3 rb = (sW * -6.0f * d * d) * r + kvec_adj(r, rl, y, c.h, (a0 * a) * fb);
+        pbi = pbi + rb;
         add3(&pbt[j], -1.0f * rb);
     }
+    atomicAdd(&lb[i], lbi);
+    add3(&pbt[i], pbi);
 }
 
 // lambda^t from p^t: adjoint of p^t (pbt) from that of lambda^t (lb).
@@ -231,7 +251,9 @@ adj_scaling_kernel(DevConsts c, const float4* __restrict__ q, const float* __res
         const F3 r = pi - f3(q[j]);
         const float r2 = dot(r, r);
         if (!in_support(c, r2)) continue;
-        const F3 g = G * kvec(r, sqrtf(r2), c.h);
+        float y;
+        const float rl = pair_length(r2, y);
+        const F3 g = G * kvec(r, rl, y, c.h);
         const float d = c.h2 - r2;
         ds += d * d * d;
         gsk += dot(g, g);
@@ -242,18 +264,21 @@ adj_scaling_kernel(DevConsts c, const float4* __restrict__ q, const float* __res
     const float rhob = (-lbar / den) / c.rho0;
     const float Db = lbar * Cc / (den * den) / c.rho0sq;
     FlatFriends f2(mt, kept_density(mt));
+    F3 pbi = {0.0f, 0.0f, 0.0f};  // particle i's own terms, added once
     for (int t = 0; t < f2.total; ++t) {
         const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
         const F3 r = pi - f3(q[j]);
         const float r2 = dot(r, r);
         if (!in_support(c, r2)) continue;
-        const float rl = sqrtf(r2);
+        float y;
+        const float rl = pair_length(r2, y);
         const float d = c.h2 - r2;
-        const F3 g = G * kvec(r, rl, c.h);
-        const F3 rb = (rhob * c.poly6 * -6.0f * d * d) * r + kvec_adj(r, rl, c.h, (G * 2.0f * Db) * (g + S));
-        add3(&pbt[i], rb);
+        const F3 g = G * kvec(r, rl, y, c.h);
+        const F3 rb = (rhob * c.poly6 * -6.0f * d * d) * r + kvec_adj(r, rl, y, c.h, (G * 2.0f * Db) * (g + S));
+        pbi = pbi + rb;
         add3(&pbt[j], -1.0f * rb);
     }
+    add3(&pbt[i], pbi);
 }
 
 // Undo the sort and the prediction p0 = x + dt (v + dt g): adjoints of the
