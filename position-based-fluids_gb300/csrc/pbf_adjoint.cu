@@ -41,6 +41,18 @@ __device__ __forceinline__ float len(F3 a) { return sqrtf(dot(a, a)); }
 
 __device__ __forceinline__ void add3(float4* a, F3 v) { atomicAdd(a, make_float4(v.x, v.y, v.z, 0.0f)); }
 
+// A friend's records as the walks below load them, four friends in flight
+// (gather_flat): its index and one or two float4 records.
+struct Friend1 {
+    uint32_t j;
+    float4 a;
+};
+struct Friend2 {
+    uint32_t j;
+    float4 a, b;
+};
+constexpr int kAdjU = 4;
+
 // k(r) and the adjoint of its argument: d/dr [k . kb] = f kb + f'(|r|)(kb.r) r/|r|
 // with f = (h-|r|)^2/|r|, f' = -(h-|r|)(h+|r|)/|r|^2.  y is 1/|r| within an
 // ulp (sqrt_recip_rn): the adjoint is an FP32 gradient, not a bit-exact one.
@@ -89,16 +101,18 @@ adj_vorticity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
     const float G = c.gradSpiky;
     F3 eta = {0.0f, 0.0f, 0.0f};
     FlatFriends f1(mt, kept_other(mt));
-    for (int t = 0; t < f1.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
-        const float4 pj = pI[j];
-        const F3 r = pi - f3(pj);
+    auto loadPO = [&](uint32_t j) {
+        j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex);
+        return Friend2{j, pI[j], omega[j]};
+    };
+    gather_flat<kAdjU>(list, n, i, f1.total, loadPO, [&](const Friend2& f) {
+        const F3 r = pi - f3(f.a);
         const float r2 = dot(r, r);
-        if (!xsph_pair(c, r2, pj.w)) continue;
+        if (!xsph_pair(c, r2, f.a.w)) return;
         float y;
         const float rl = pair_length(r2, y);
-        eta = eta + len(f3(omega[j])) * kvec(r, rl, y, c.h);
-    }
+        eta = eta + len(f3(f.b)) * kvec(r, rl, y, c.h);
+    });
     eta = -G * eta;
     const float l = len(eta);
     if (!(l > 0.0f)) return;
@@ -110,22 +124,20 @@ adj_vorticity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
     const F3 etab = (1.0f / l) * (Nb - dot(N, Nb) * N);
     FlatFriends f2(mt, kept_other(mt));
     F3 pbi = {0.0f, 0.0f, 0.0f};  // particle i's own terms, added once
-    for (int t = 0; t < f2.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
-        const float4 pj = pI[j];
-        const F3 r = pi - f3(pj);
+    gather_flat<kAdjU>(list, n, i, f2.total, loadPO, [&](const Friend2& f) {
+        const F3 r = pi - f3(f.a);
         const float r2 = dot(r, r);
-        if (!xsph_pair(c, r2, pj.w)) continue;
+        if (!xsph_pair(c, r2, f.a.w)) return;
         float y;
         const float rl = pair_length(r2, y);
         const F3 k = kvec(r, rl, y, c.h);
-        const F3 oj = f3(omega[j]);
+        const F3 oj = f3(f.b);
         const float ol = len(oj);
-        if (ol > 0.0f) add3(&omb[j], (-G * dot(etab, k) / ol) * oj);
+        if (ol > 0.0f) add3(&omb[f.j], (-G * dot(etab, k) / ol) * oj);
         const F3 rb = kvec_adj(r, rl, y, c.h, (-G * ol) * etab);
         pbi = pbi + rb;
-        add3(&pb[j], -1.0f * rb);
-    }
+        add3(&pb[f.j], -1.0f * rb);
+    });
     add3(&pb[i], pbi);
 }
 
@@ -145,15 +157,18 @@ adj_viscosity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
         const float G = c.gradSpiky;
         F3 v2bi = v3b, pbi = {0.0f, 0.0f, 0.0f};  // particle i's own terms, added once
         FlatFriends fr(mt, kept_other(mt));
-        for (int t = 0; t < fr.total; ++t) {
-            const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
-            const float4 pj = pI[j];
-            const F3 r = pi - f3(pj);
+        auto loadPV = [&](uint32_t j) {
+            j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex);
+            return Friend2{j, pI[j], v2[j]};
+        };
+        gather_flat<kAdjU>(list, n, i, fr.total, loadPV, [&](const Friend2& f) {
+            const uint32_t j = f.j;
+            const F3 r = pi - f3(f.a);
             const float r2 = dot(r, r);
-            if (!xsph_pair(c, r2, pj.w)) continue;
+            if (!xsph_pair(c, r2, f.a.w)) return;
             float y;
             const float rl = pair_length(r2, y);
-            const F3 u = f3(v2[j]) - vi;
+            const F3 u = f3(f.b) - vi;
             const float d = c.h2 - r2;
             const float w = c.poly6 * d * d * d;
             const F3 k = kvec(r, rl, y, c.h);
@@ -165,7 +180,7 @@ adj_viscosity_kernel(DevConsts c, const float4* __restrict__ pI, const float4* _
             const F3 rb = (Wb * -6.0f * d * d) * r + kvec_adj(r, rl, y, c.h, (-G) * cross(ob, u));
             pbi = pbi + rb;
             add3(&pb[j], -1.0f * rb);
-        }
+        });
         add3(&v2b[i], v2bi);
         add3(&pb[i], pbi);
     }
@@ -207,12 +222,16 @@ adj_delta_kernel(DevConsts c, const float4* __restrict__ q, const uint8_t* __res
     const float a0 = -c.gradSpiky / c.rho0;
     const uint64_t mt = load_meta(meta, i);
     FlatFriends fr(mt, kept_other(mt));
-    for (int t = 0; t < fr.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
-        const float4 qj = q[j];
+    auto loadQ = [&](uint32_t j) {
+        j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex);
+        return Friend1{j, q[j]};
+    };
+    gather_flat<kAdjU>(list, n, i, fr.total, loadQ, [&](const Friend1& f) {
+        const uint32_t j = f.j;
+        const float4 qj = f.a;
         const F3 r = pi - f3(qj);
         const float r2 = dot(r, r);
-        if (!in_support(c, r2)) continue;
+        if (!in_support(c, r2)) return;
         float y;
         const float rl = pair_length(r2, y);
         const float d = c.h2 - r2;
@@ -226,7 +245,7 @@ adj_delta_kernel(DevConsts c, const float4* __restrict__ q, const uint8_t* __res
         const F3 rb = (sW * -6.0f * d * d) * r + kvec_adj(r, rl, y, c.h, (a0 * a) * fb);
         pbi = pbi + rb;
         add3(&pbt[j], -1.0f * rb);
-    }
+    });
     atomicAdd(&lb[i], lbi);
     add3(&pbt[i], pbi);
 }
@@ -246,11 +265,14 @@ adj_scaling_kernel(DevConsts c, const float4* __restrict__ q, const float* __res
     float ds = 0.0f, gsk = 0.0f;
     F3 S = {0.0f, 0.0f, 0.0f};
     FlatFriends f1(mt, kept_density(mt));
-    for (int t = 0; t < f1.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
-        const F3 r = pi - f3(q[j]);
+    auto loadQ = [&](uint32_t j) {
+        j = checked_index(j, (uint32_t)n, c.err, kErrFriendIndex);
+        return Friend1{j, q[j]};
+    };
+    gather_flat<kAdjU>(list, n, i, f1.total, loadQ, [&](const Friend1& f) {
+        const F3 r = pi - f3(f.a);
         const float r2 = dot(r, r);
-        if (!in_support(c, r2)) continue;
+        if (!in_support(c, r2)) return;
         float y;
         const float rl = pair_length(r2, y);
         const F3 g = G * kvec(r, rl, y, c.h);
@@ -258,18 +280,18 @@ adj_scaling_kernel(DevConsts c, const float4* __restrict__ q, const float* __res
         ds += d * d * d;
         gsk += dot(g, g);
         S = S + g;
-    }
+    });
     const float rho = ds * c.poly6, D = gsk + dot(S, S);
     const float den = D / c.rho0sq + c.eps, Cc = rho / c.rho0 - 1.0f;
     const float rhob = (-lbar / den) / c.rho0;
     const float Db = lbar * Cc / (den * den) / c.rho0sq;
     FlatFriends f2(mt, kept_density(mt));
     F3 pbi = {0.0f, 0.0f, 0.0f};  // particle i's own terms, added once
-    for (int t = 0; t < f2.total; ++t) {
-        const uint32_t j = checked_index(list[(size_t)t * n + i], (uint32_t)n, c.err, kErrFriendIndex);
-        const F3 r = pi - f3(q[j]);
+    gather_flat<kAdjU>(list, n, i, f2.total, loadQ, [&](const Friend1& f) {
+        const uint32_t j = f.j;
+        const F3 r = pi - f3(f.a);
         const float r2 = dot(r, r);
-        if (!in_support(c, r2)) continue;
+        if (!in_support(c, r2)) return;
         float y;
         const float rl = pair_length(r2, y);
         const float d = c.h2 - r2;
@@ -277,7 +299,7 @@ adj_scaling_kernel(DevConsts c, const float4* __restrict__ q, const float* __res
         const F3 rb = (rhob * c.poly6 * -6.0f * d * d) * r + kvec_adj(r, rl, y, c.h, (G * 2.0f * Db) * (g + S));
         pbi = pbi + rb;
         add3(&pbt[j], -1.0f * rb);
-    }
+    });
     add3(&pbt[i], pbi);
 }
 
