@@ -197,7 +197,9 @@ int pbf_read_state_async(pbf_ctx* ctx, float* pos, float* vel, float* pred);
    with the same results, but the position copy overlaps the last substep:
    positions are final after updateVelocities (update_velocities.cl), so they
    are copied on a second stream while applyViscosity and applyVorticity run.
-   The velocity copy follows applyVorticity.  The reference's frame loop
+   With both pointers given, applyVorticity runs in two launches over the two
+   halves of the particles, and the first half's velocities are copied while
+   the second half runs; the rest follows it.  The reference's frame loop
    (src/Runner.cpp:118-130) steps and then hands positions to the renderer;
    this call is that frame for a host-memory consumer.  Either pointer may be
    NULL; page-locked memory is needed for the overlap.  With stage timing on,

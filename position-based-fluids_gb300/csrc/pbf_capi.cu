@@ -86,9 +86,11 @@ struct pbf_ctx {
     bool stepped = false;
 
     // pbf_step_read_async: the last substep copies its final positions out on
-    // copyStream while XSPH and vorticity run, and its velocities after them
+    // copyStream while XSPH and vorticity run, and its velocities in two
+    // parts: the first half's on copyStream while the vorticity pass runs
+    // over the second half, the rest after it
     cudaStream_t copyStream = nullptr;
-    cudaEvent_t evPosReady = nullptr, evCopyDone = nullptr;
+    cudaEvent_t evPosReady = nullptr, evCopyDone = nullptr, evVelHead = nullptr;
     float* readPos = nullptr;
     float* readVel = nullptr;
 
@@ -490,6 +492,7 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     const int P = ctx->curPos, V = ctx->curVel;
     uint64_t launched = 0;
     bool rangeOpen = false;
+    bool velCopied = false;  // the read-back's velocities, copied in two parts around a split vorticity pass
     auto mark = [&](const char* name, int iteration = -1) {
         if (ctx->nvtx) {  // one range per stage, named as its tracker
             if (rangeOpen) nvtxRangePop();
@@ -591,11 +594,31 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     pbf::launch_apply_viscosity(c, b, ctx->pred[a], ctx->vel[V], ctx->vel[V ^ 1], omega, list, meta, flat, ls.viscosity,
                                 ls.balance, tiles(3), s);
     mark("applyVorticity");
-    pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, flat, ls.vorticity,
-                                ls.balance, tiles(4), s);
+    const int vortTiles = (c.n + ls.vorticity - 1) / ls.vorticity;
+    if (ctx->readVel && ctx->readPos && vortTiles >= 2) {
+        // the first half of the particles' velocities copy out while the second half runs
+        const int half = vortTiles / 2;
+        const size_t headBytes = 16 * (size_t)half * (size_t)ls.vorticity;
+        pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, flat,
+                                    ls.vorticity, ls.balance, nullptr, s, 0, half);
+        PBF_CUDA(ctx, cudaEventRecord(ctx->evVelHead, s));
+        PBF_CUDA(ctx, cudaStreamWaitEvent(ctx->copyStream, ctx->evVelHead, 0));
+        PBF_CUDA(ctx, cudaMemcpyAsync(ctx->readVel, ctx->vel[V], headBytes, cudaMemcpyDeviceToHost, ctx->copyStream));
+        PBF_CUDA(ctx, cudaEventRecord(ctx->evCopyDone, ctx->copyStream));
+        pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, flat,
+                                    ls.vorticity, ls.balance, nullptr, s, half, vortTiles - half);
+        PBF_CUDA(ctx, cudaMemcpyAsync(reinterpret_cast<char*>(ctx->readVel) + headBytes,
+                                      reinterpret_cast<const char*>(ctx->vel[V]) + headBytes, v4 - headBytes,
+                                      cudaMemcpyDeviceToHost, s));
+        velCopied = true;
+        ++launched;
+    } else {
+        pbf::launch_apply_vorticity(c, ctx->pred[a], omega, ctx->vel[V ^ 1], ctx->vel[V], list, meta, flat,
+                                    ls.vorticity, ls.balance, tiles(4), s);
+    }
     launched += 3;
     if (rangeOpen) nvtxRangePop();
-    if (ctx->readVel) PBF_CUDA(ctx, cudaMemcpyAsync(ctx->readVel, ctx->vel[V], v4, cudaMemcpyDeviceToHost, s));
+    if (ctx->readVel && !velCopied) PBF_CUDA(ctx, cudaMemcpyAsync(ctx->readVel, ctx->vel[V], v4, cudaMemcpyDeviceToHost, s));
     if (ctx->readPos) PBF_CUDA(ctx, cudaStreamWaitEvent(s, ctx->evCopyDone, 0));  // later work waits for the copy
     PBF_CUDA(ctx, cudaGetLastError());
     ctx->curPos = sortedPos ^ 1;
@@ -906,6 +929,7 @@ int pbf_destroy(pbf_ctx* ctx) {
     if (ctx->timingAnchor) cudaEventDestroy(ctx->timingAnchor);
     if (ctx->evPosReady) cudaEventDestroy(ctx->evPosReady);
     if (ctx->evCopyDone) cudaEventDestroy(ctx->evCopyDone);
+    if (ctx->evVelHead) cudaEventDestroy(ctx->evVelHead);
     if (ctx->copyStream) cudaStreamDestroy(ctx->copyStream);
     free_render(ctx);
     free_rollout(ctx);
@@ -1341,6 +1365,7 @@ int pbf_step_read_async(pbf_ctx* ctx, int substeps, float* pos, float* vel) {
         if (!ctx->copyStream) PBF_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copyStream, cudaStreamNonBlocking));
         if (!ctx->evPosReady) PBF_CUDA(ctx, cudaEventCreateWithFlags(&ctx->evPosReady, cudaEventDisableTiming));
         if (!ctx->evCopyDone) PBF_CUDA(ctx, cudaEventCreateWithFlags(&ctx->evCopyDone, cudaEventDisableTiming));
+        if (!ctx->evVelHead) PBF_CUDA(ctx, cudaEventCreateWithFlags(&ctx->evVelHead, cudaEventDisableTiming));
     }
     ctx->readPos = pos;
     ctx->readVel = vel;

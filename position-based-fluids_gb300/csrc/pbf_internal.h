@@ -144,9 +144,13 @@ void launch_update_velocities(const DevConsts& c, const float4* pred, const floa
 void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, const float4* velIn, float4* velOut,
                             float4* omega, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
                             int balance, int* tileCounter, cudaStream_t s);
+// tileCount > 0: only the particle tiles [firstTile, firstTile + tileCount)
+// of `block` particles, one block per tile (a frame's read-back splits the
+// last vorticity pass so that the first part's velocities copy out while the
+// rest runs).
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
                             float4* velOut, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
-                            int balance, int* tileCounter, cudaStream_t s);
+                            int balance, int* tileCounter, cudaStream_t s, int firstTile = 0, int tileCount = 0);
 
 // ---- radix sort (pbf_sort.cu) ----
 struct SortPlan {

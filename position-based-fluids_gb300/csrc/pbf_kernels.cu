@@ -1030,8 +1030,9 @@ __global__ void __launch_bounds__(kMaxBlock)
 apply_vorticity_kernel(DevConsts c, const float4* __restrict__ pred, const float4* __restrict__ omega,
                        const float4* __restrict__ velIn, float4* __restrict__ velOut,
                        const uint32_t* __restrict__ list, const uint2* __restrict__ meta,
-                       const uint32_t* __restrict__ flatIn, int tiles, int* tileCounter) {
+                       const uint32_t* __restrict__ flatIn, int tiles, int* tileCounter, int tileOffset) {
     for_tiles(tiles, tileCounter, [&](int tile) {
+        tile += tileOffset;  // a launch over part of the tiles (one block per tile)
         const int i = B ? balanced_particle(meta, c.n, false, tile) : tile * (int)blockDim.x + (int)threadIdx.x;
         if (i < 0 || i >= c.n) return;
         const float4 pi = pred[i];
@@ -1184,12 +1185,16 @@ void launch_apply_viscosity(const DevConsts& c, Batch b, const float4* pred, con
 
 void launch_apply_vorticity(const DevConsts& c, const float4* pred, const float4* omega, const float4* velIn,
                             float4* velOut, const uint32_t* list, const uint2* meta, const uint32_t* flatIn, int block,
-                            int balance, int* tileCounter, cudaStream_t s) {
+                            int balance, int* tileCounter, cudaStream_t s, int firstTile, int tileCount) {
     auto k = c.relaxed ? (balance ? apply_vorticity_kernel<true, true, kWalkFlat> : apply_vorticity_kernel<true, false, kWalkFlat>)
                        : (balance ? apply_vorticity_kernel<false, true, kWalkFlat> : apply_vorticity_kernel<false, false, kWalkFlat>);
+    if (tileCount > 0) {  // tiles [firstTile, firstTile + tileCount), one block each
+        k<<<(unsigned)tileCount, block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta, flatIn, 0, nullptr, firstTile);
+        return;
+    }
     int tiles = 0;
     const unsigned grid = grid_for_tiles(k, c.n, block, tileCounter != nullptr, &tiles);
-    k<<<grid, block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta, flatIn, tiles, tileCounter);
+    k<<<grid, block, 0, s>>>(c, pred, omega, velIn, velOut, list, meta, flatIn, tiles, tileCounter, 0);
 }
 
 }  // namespace pbf
