@@ -42,6 +42,18 @@ def test_library_exports_only_the_declared_c_abi(built_lib):
     assert exported == declared_functions()
 
 
+def test_build_tracks_every_header():
+    """A unit is rebuilt when any header it may include changes, device
+    headers (.cuh) included: an edit there must not leave stale objects."""
+    from tests.conftest import load_pkg_build
+    pkg_build = load_pkg_build()
+    tracked = {h.name for h in pkg_build._headers()}
+    csrc = REPO / "position-based-fluids_gb300" / "csrc"
+    headers = {h.name for pattern in ("*.h", "*.cuh") for h in csrc.glob(pattern)}
+    headers |= {h.name for h in (REPO / "include").glob("*.h")}
+    assert headers and headers <= tracked, f"untracked headers: {sorted(headers - tracked)}"
+
+
 def test_checked_build_exports_the_same_symbols():
     """The bounds-checked build (build.py --checked) is a drop-in for the plain
     library: built from the same sources with -DPBF_CHECK_BOUNDS into its own
