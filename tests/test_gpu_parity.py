@@ -183,18 +183,20 @@ def test_substeps_bit_exact(name, algorithm, pbf_mod, oracle_mod, cuda_device):
     assert_same("pred", gpr, opr)
 
 
-def test_tiny_coordinates_bit_exact(pbf_mod, oracle_mod, cuda_device):
+@pytest.mark.parametrize("algorithm", [0, 1, 2], ids=["scan", "warp", "brick"])
+def test_tiny_coordinates_bit_exact(algorithm, pbf_mod, oracle_mod, cuda_device):
     """Predicted coordinates in (0, 2^-27): their differences can be too small
     for the exact passes' quotients through one reciprocal, so the particles
     that may hold such a friend (the 27 cells around it) divide the IEEE way
     for the rest of the substep.  A block at the origin (no clamp) with some
-    particles moved onto tiny coordinates next to neighbours at exactly 0."""
+    particles moved onto tiny coordinates next to neighbours at exactly 0;
+    each friends build records the cells the taint kernel marks."""
     params, pos, vel = scene(pbf_mod, (10, 10, 10), origin=(0.0, 0.0, 0.0), jitter=0.0, boxClamp=0)
     pos[1, 0] = np.float32(3e-13)       # x next to particle 0 at x = 0
     pos[10, 1] = np.float32(1e-30)      # y, a normal float far below 2^-27
     pos[100, 2] = np.float32(2e-42)     # z, subnormal
     pos[111, :3] = np.float32(5e-39)
-    gp, gv, gpr, gcounts, glist = run_gpu(pbf_mod, params, pos, vel, 3, cuda_device)
+    gp, gv, gpr, gcounts, glist = run_gpu(pbf_mod, params, pos, vel, 3, cuda_device, algorithm=algorithm)
     op, ov, opr, dbg = oracle_mod.step(params, pos, vel, 3, debug=True)
     assert np.array_equal(gcounts, dbg["counts"]), "friend counts"
     assert_same("pos", gp, op)
