@@ -661,7 +661,7 @@ __device__ __forceinline__ void compute_scaling_body(const DevConsts& c, const f
     // complete neighbour sets count the particle itself first: d = h^2 - 0
     float ds = c.complete ? c.h2 * c.h2 * c.h2 : 0.0f, gsk = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
     constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
-    gather_walk<W, U>(list, flatIn, flatOut, n, i, FriendRows(mt, kept_density(mt), c.perCircle),
+    gather_walk<W, U, true>(list, flatIn, flatOut, n, i, FriendRows(mt, kept_density(mt), c.perCircle),
                       [&](uint32_t j) { return __ldg(pred + checked_index(j, (uint32_t)n, c.err, kErrFriendIndex)); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         if (R) {
@@ -746,7 +746,7 @@ __device__ __forceinline__ void compute_delta_body(const DevConsts& c, const Bat
     const int n = c.n;
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     constexpr int U = 4;  // friends in flight: the passes wait on their neighbour gathers (long scoreboard)
-    gather_walk<W, U>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
+    gather_walk<W, U, true>(list, flatIn, nullptr, n, i, FriendRows(mt, kept_other(mt), c.perCircle),
                       [&](uint32_t j) { return __ldg(pp + checked_index(j, (uint32_t)n, c.err, kErrFriendIndex)); }, [&](const float4 pj) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
         if (R) {
