@@ -53,7 +53,7 @@ struct pbf_ctx {
     uint2* meta = nullptr;       // per-particle friend counts per circle + kept circles
     uint32_t* taint = nullptr;          // per particle: the substep that tainted it (pbf::DevConsts::taint)
     int4* cellXYZ = nullptr;            // per particle: its cell at the friends build and the scene's first key
-    uint32_t* irregularList = nullptr;  // particles found at irregular positions (pbf::DevConsts::irregularList)
+    uint32_t* cellStart = nullptr;      // per cell key: its first particle (pbf::DevConsts::cellStart)
     int* errWord = nullptr;
     int* tileCounters = nullptr;  // 2 words per neighbour kernel: its persistent grid's tile counter
     size_t histWords = 0;
@@ -333,11 +333,10 @@ void apply_planes(pbf_ctx* ctx) {
     ctx->consts.wave = ctx->waveDev;
     ctx->consts.err = ctx->errWord;
     ctx->consts.epoch = reinterpret_cast<uint32_t*>(ctx->errWord + 1);
-    ctx->consts.irregularCount = reinterpret_cast<uint32_t*>(ctx->errWord + 2);
     ctx->consts.taint = ctx->taint;
-    ctx->consts.cellXYZ = ctx->cellXYZ;
-    // the record of irregular positions: exact mode (relaxed passes divide no way but their own)
-    ctx->consts.irregularList = ctx->consts.relaxed ? nullptr : ctx->irregularList;
+    // the cells of irregular positions: exact mode (relaxed passes divide no way but their own)
+    ctx->consts.cellXYZ = ctx->consts.relaxed ? nullptr : ctx->cellXYZ;
+    ctx->consts.cellStart = ctx->cellStart;
 }
 
 // The captured substep; the reverse pass's segment graphs are dropped with
@@ -538,19 +537,13 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
     if (tape) PBF_CUDA(ctx, cudaMemcpyAsync(tape->perm, ctx->perm[ctx->keysIdx], 4 * (size_t)c.n, cudaMemcpyDeviceToDevice, s));
     mark("updateCells");
     const uint32_t tableKeys = ctx->cellsWords * (uint32_t)(is_batch(ctx) ? ctx->sceneParams.size() : 1);
-    pbf::launch_update_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s);
+    c.keys = keys;  // the taint of irregular positions finds a cell's particles in them
+    pbf::launch_update_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s, ctx->cellStart);
     mark("buildFriendsList");
     // the flat rows of the kept friends: written by the staged build, else
     // recorded by the first density pass (or flattened when there is none)
     bool haveFlat = pbf::launch_build_friends(c, b, ctx->pred[sortedPred], ctx->cells, list, flat, meta, ctx->errWord,
                                               ls.friends, ls.friendsAlgorithm, s);
-    // the particles next to irregular positions divide the IEEE way (pbf::quotients_tainted)
-    auto taint = [&]() {
-        if (!c.irregularList) return;
-        pbf::launch_taint_neighbours(c, keys, s);
-        ++launched;
-    };
-    taint();
     mark("resetPartList");
     pbf::launch_reset_cells(c.n, keys, ctx->cells, tableKeys, ctx->errWord, s);
     launched += 3;
@@ -568,7 +561,6 @@ int enqueue_substep(pbf_ctx* ctx, StageClock* clock, const pbf::AdjointTape* tap
                                   it + 1 == iters, tape && tape->mask ? tape->mask + (size_t)it * c.n : nullptr,
                                   flat, ls.delta, ls.balance, tiles(2), s);
         launched += 2;
-        taint();
     }
     if (!haveFlat) {
         pbf::launch_flatten_friends(c, list, meta, flat, s);
@@ -902,10 +894,9 @@ int pbf_create(const PbfParameters* params, int device, pbf_ctx** out) {
     ctx->device = device;
     PBF_CUDA(nullptr, cudaSetDevice(device));
     PBF_CUDA(nullptr, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-    // [0]: the error word; [1]: the substep counter of the taint marks (pbf::DevConsts::epoch);
-    // [2]: the number of recorded irregular positions (pbf::DevConsts::irregularCount)
-    PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->errWord, 3 * sizeof(int)));
-    PBF_CUDA(nullptr, cudaMemset(ctx->errWord, 0, 3 * sizeof(int)));
+    // [0]: the error word; [1]: the substep counter of the taint marks (pbf::DevConsts::epoch)
+    PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->errWord, 2 * sizeof(int)));
+    PBF_CUDA(nullptr, cudaMemset(ctx->errWord, 0, 2 * sizeof(int)));
     PBF_CUDA(nullptr, cudaMalloc((void**)&ctx->tileCounters, 10 * sizeof(int)));
     PBF_CUDA(nullptr, cudaMemset(ctx->tileCounters, 0, 10 * sizeof(int)));
     *out = ctx.release();
@@ -923,7 +914,7 @@ int pbf_destroy(pbf_ctx* ctx) {
     }
     dev_free(ctx->omega); dev_free(ctx->density); dev_free(ctx->hist); dev_free(ctx->cells);
     dev_free(ctx->list); dev_free(ctx->flat); dev_free(ctx->meta); dev_free(ctx->errWord); dev_free(ctx->tileCounters);
-    dev_free(ctx->taint); dev_free(ctx->cellXYZ); dev_free(ctx->irregularList);
+    dev_free(ctx->taint); dev_free(ctx->cellXYZ); dev_free(ctx->cellStart);
     dev_free(ctx->scenes); dev_free(ctx->sceneOf); dev_free(ctx->ids); dev_free(ctx->idsTmp);
     dev_free(ctx->quadsDev); dev_free(ctx->maskDev); dev_free(ctx->waveDev);
     if (ctx->timingAnchor) cudaEventDestroy(ctx->timingAnchor);
@@ -1021,12 +1012,13 @@ int pbf_init_cells(pbf_ctx* ctx) {
     if ((rc = dev_alloc(ctx, &ctx->list, (size_t)ctx->listSlots * ctx->n)) ||
         (rc = dev_alloc(ctx, &ctx->flat, (size_t)ctx->listSlots * ctx->n)) || (rc = dev_alloc(ctx, &ctx->meta, ctx->n)) ||
         (rc = dev_alloc(ctx, &ctx->taint, ctx->n)) || (rc = dev_alloc(ctx, &ctx->cellXYZ, ctx->n)) ||
-        (rc = dev_alloc(ctx, &ctx->irregularList, ctx->n)))
+        (rc = dev_alloc(ctx, &ctx->cellStart, tableWords)))
         return rc;
     PBF_CUDA(ctx, cudaMemset(ctx->meta, 0, 8 * (size_t)ctx->n));
-    // taint marks are substep numbers from 1 on (the counter restarts with them); no record pending
+    // taint marks are substep numbers from 1 on (the counter restarts with them); no cell start yet
     PBF_CUDA(ctx, cudaMemset(ctx->taint, 0, 4 * (size_t)ctx->n));
-    PBF_CUDA(ctx, cudaMemset(ctx->errWord + 1, 0, 2 * sizeof(int)));
+    PBF_CUDA(ctx, cudaMemset(ctx->errWord + 1, 0, sizeof(int)));
+    PBF_CUDA(ctx, cudaMemset(ctx->cellStart, 0xFF, 4 * tableWords));
     apply_planes(ctx);
     ctx->cellsReady = true;
     ctx->kernelsReady = false;

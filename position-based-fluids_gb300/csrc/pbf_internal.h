@@ -55,8 +55,9 @@ struct DevConsts {
     uint32_t* epoch;             // device word: the substep's number, counted by the predict kernel
     uint32_t* taint;             // per particle: the last substep that tainted it (quotients_tainted)
     int4* cellXYZ;               // per particle: the cell its friends were taken around, and the scene's first key
-    uint32_t* irregularList;     // particles found at irregular positions by the last writing kernel
-    uint32_t* irregularCount;    // device word: their number (the taint kernel resets it)
+                                 // (NULL in relaxed mode: nothing is tainted)
+    const uint32_t* cellStart;   // per cell key: its first particle, when the substep's keys confirm it
+    const uint32_t* keys;        // the substep's sorted cell keys (set per substep)
     int circles, perCircle;
     uint32_t grid;
     int n;
@@ -111,12 +112,9 @@ void launch_compute_keys(const DevConsts& c, Batch b, const float4* pred, uint32
 // permutation entries or keys to; keyLimit: the number of cell-table entries.
 void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const float4* pred, const uint32_t* ids,
                           float4* posOut, float4* predOut, uint32_t* idsOut, int* err, cudaStream_t s);
-void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
-// Taints, for the rest of the substep, every particle of the 27 cells around
-// each particle recorded at an irregular position since the last call
-// (DevConsts::irregularList), and empties the record.  keys: the substep's
-// sorted cell keys.
-void launch_taint_neighbours(const DevConsts& c, const uint32_t* keys, cudaStream_t s);
+// cellStart (may be NULL): also each occupied cell's first particle.
+void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s,
+                         uint32_t* cellStart = nullptr);
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s);
 // tileCounter (two device words, zero between launches; NULL for one block
 // per tile of particles): the solver passes' persistent grid, whose

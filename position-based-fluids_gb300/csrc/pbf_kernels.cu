@@ -106,8 +106,10 @@ __global__ void gather_sorted_kernel(int n, const uint32_t* __restrict__ perm, c
 
 // --------------------------------------------------------------- cells --
 // update_cells.cl:6-25 on a table that holds END_OF_CELL_LIST everywhere.
+// cellStart (may be NULL) also receives each occupied cell's first particle;
+// it is never reset (taint_around checks an entry against the keys).
 __global__ void update_cells_kernel(int n, const uint32_t* __restrict__ keys, uint32_t* __restrict__ cells,
-                                    uint32_t keyLimit, int* err) {
+                                    uint32_t keyLimit, int* err, uint32_t* __restrict__ cellStart) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t k = checked_index(keys[i], keyLimit, err, kErrCellKey);
@@ -116,50 +118,13 @@ __global__ void update_cells_kernel(int n, const uint32_t* __restrict__ keys, ui
         if (kp != k) {
             cells[2 * (size_t)k] = (uint32_t)i;
             cells[2 * (size_t)kp + 1] = (uint32_t)(i - 1);
+            if (cellStart) cellStart[k] = (uint32_t)i;
         }
         if (i == n - 1) cells[2 * (size_t)k + 1] = (uint32_t)i;
     } else {
         cells[2 * (size_t)k] = 0u;
+        if (cellStart) cellStart[k] = 0u;
     }
-}
-
-// The first index of the sorted keys at or above k, found by a whole warp:
-// each step probes 32 evenly spaced keys of the interval that holds the
-// answer and keeps the 1/32 of it between the last probe below k and the
-// next, so 2^20 keys take four dependent loads.
-__device__ __forceinline__ uint32_t warp_lower_bound(const uint32_t* __restrict__ keys, uint32_t n, uint32_t k,
-                                                     uint32_t lane) {
-    uint32_t lo = 0, hi = n;  // the answer lies in [lo, hi]
-    while (hi - lo > 32u) {
-        const uint32_t step = (hi - lo + 31u) / 32u;
-        const uint32_t probe = lo + lane * step;
-        const uint32_t below = __popc(__ballot_sync(0xFFFFFFFFu, probe < hi && keys[probe] < k));
-        if (below == 0u) return lo;
-        const uint32_t next = lo + below * step;
-        lo = lo + (below - 1u) * step + 1u;
-        hi = min(hi, next);
-    }
-    return lo + __popc(__ballot_sync(0xFFFFFFFFu, lo + lane < hi && keys[lo + lane] < k));
-}
-
-// Every particle of the 27 cells around each particle recorded at an
-// irregular position (DevConsts::irregularList), tainted for the rest of the
-// substep; a cell's particles are the run of its key in the sorted keys.  One
-// block of 32 warps, a warp per (recorded particle, cell), which then empties
-// the record for the next writer.
-constexpr int kTaintThreads = 1024;
-__global__ void __launch_bounds__(kTaintThreads) taint_neighbours_kernel(DevConsts c, const uint32_t* __restrict__ keys) {
-    const uint32_t count = *c.irregularCount, e = *c.epoch, n = (uint32_t)c.n;
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    for (uint32_t pair = warp; pair < 27u * count; pair += kTaintThreads / 32) {
-        const int4 q = c.cellXYZ[c.irregularList[pair / 27u]];
-        const int k = (int)(pair % 27u);
-        const uint32_t key = (uint32_t)q.w + grid_hash(q.x + k / 9 - 1, q.y + (k / 3) % 3 - 1, q.z + k % 3 - 1, c.grid);
-        const uint32_t first = warp_lower_bound(keys, n, key, lane), end = warp_lower_bound(keys, n, key + 1u, lane);
-        for (uint32_t p = first + lane; p < end; p += 32u) c.taint[p] = e;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) *c.irregularCount = 0u;
 }
 
 // reset_grid.cl:6-14
@@ -1061,12 +1026,9 @@ void launch_gather_sorted(int n, const uint32_t* perm, const float4* pos, const 
     gather_sorted_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, perm, pos, pred, ids, posOut, predOut, idsOut, err);
 }
 
-void launch_taint_neighbours(const DevConsts& c, const uint32_t* keys, cudaStream_t s) {
-    taint_neighbours_kernel<<<1, kTaintThreads, 0, s>>>(c, keys);
-}
-
-void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s) {
-    update_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, cells, keyLimit, err);
+void launch_update_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s,
+                         uint32_t* cellStart) {
+    update_cells_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, keys, cells, keyLimit, err, cellStart);
 }
 
 void launch_reset_cells(int n, const uint32_t* keys, uint32_t* cells, uint32_t keyLimit, int* err, cudaStream_t s) {
