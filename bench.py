@@ -96,19 +96,20 @@ STAGE_BYTES = {
 # and the mean over the four launches of each solver pass in the substep (for
 # the density pass: the one that records the flat friend rows and three that
 # read them).  Launch shape of the capture: the autotuner's for that state
-# under ncu (friends 256-thread blocks, solver passes 128, plain thread map).
+# under ncu (friends 128-thread blocks, density passes 128, position passes
+# 64, plain thread map).
 # Scaled to the measured list lengths: the traffic by the stage's
 # list-inclusive bytes, the instructions in proportion to the list length of
 # the pass (for the friends build, whose candidates grow with the density,
 # to nl).
-CAPTURE_SOURCE = ("ncu capture of the first substep of frame 51 (friends 256-thread blocks, solver passes 128, "
-                  "list lengths 38.52 / 32.79), scaled by list length")
-TRAFFIC_CAPTURE = {"buildFriendsList": {"bytes": 801.8e6, "nl": 38.52, "nd": 32.79},
-                   "computeScaling": {"bytes": 317.6e6, "nl": 38.52, "nd": 32.79},
-                   "computeDelta": {"bytes": 224.7e6, "nl": 38.52, "nd": 32.79}}
+CAPTURE_SOURCE = ("ncu capture of the first substep of frame 51 (friends 128-thread blocks, density passes 128, "
+                  "position passes 64, list lengths 38.52 / 32.79), scaled by list length")
+TRAFFIC_CAPTURE = {"buildFriendsList": {"bytes": 813.3e6, "nl": 38.52, "nd": 32.79},
+                   "computeScaling": {"bytes": 308.8e6, "nl": 38.52, "nd": 32.79},
+                   "computeDelta": {"bytes": 216.4e6, "nl": 38.52, "nd": 32.79}}
 ISSUE_CAPTURE = {"buildFriendsList": {"inst": 650.0e6, "nl": 38.52, "nd": 32.79},
                  "computeScaling": {"inst": 114.5e6, "nl": 38.52, "nd": 32.79},
-                 "computeDelta": {"inst": 116.5e6, "nl": 38.52, "nd": 32.79}}
+                 "computeDelta": {"inst": 116.6e6, "nl": 38.52, "nd": 32.79}}
 SM_COUNT = 152
 SCHEDULERS_PER_SM = 4
 
