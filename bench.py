@@ -658,16 +658,20 @@ def gpu_arm(args) -> None:
     density_error = {"mean": float(rel.mean()), "p95": float(np.percentile(rel, 95)), "max": float(rel.max()),
                      "note": "|rho / rho0 - 1| per particle, density of the last solver iteration"}
 
-    issue = None
-    if dominant in ISSUE_CAPTURE and (args.math == "exact" or dominant == "buildFriendsList"):
-        cap = ISSUE_CAPTURE[dominant]
-        inst = cap["inst"] * (nl / cap["nl"] if dominant in ("computeScaling", "buildFriendsList") else nd / cap["nd"])
-        clk = clocks.summary().get("sm_mhz") or 2070.0
-        peak_issue = SM_COUNT * SCHEDULERS_PER_SM * clk * 1e6
-        issue = {"kernel": dominant, "warp_instructions_per_launch": inst,
-                 "achieved": inst / (launch_ms / 1000.0), "peak": peak_issue, "unit": "warp instructions/s",
-                 "frac": inst / (launch_ms / 1000.0) / peak_issue,
-                 "source": "smsp__inst_executed.sum of the " + CAPTURE_SOURCE}
+    # the issue rate of every captured stage (the exact passes' bound), the dominant one as issue_roofline
+    clk = clocks.summary().get("sm_mhz") or 2070.0
+    peak_issue = SM_COUNT * SCHEDULERS_PER_SM * clk * 1e6
+    stage_issue = {}
+    for k, cap in ISSUE_CAPTURE.items():
+        if k not in stage_ms or (args.math != "exact" and k != "buildFriendsList"):
+            continue
+        inst = cap["inst"] * (nl / cap["nl"] if k in ("computeScaling", "buildFriendsList") else nd / cap["nd"])
+        k_ms = stage_ms[k] / launches_per_frame(k, iters, sub)
+        stage_issue[k] = {"kernel": k, "warp_instructions_per_launch": inst, "ms_per_launch": k_ms,
+                          "achieved": inst / (k_ms / 1000.0), "peak": peak_issue, "unit": "warp instructions/s",
+                          "frac": inst / (k_ms / 1000.0) / peak_issue,
+                          "source": "smsp__inst_executed.sum of the " + CAPTURE_SOURCE}
+    issue = stage_issue.get(dominant)
 
     # ---- the other arithmetic mode, same start state, its own block sizes ----
     other_line = None
@@ -732,6 +736,7 @@ def gpu_arm(args) -> None:
         "pipeline_roofline": {"bytes_per_particle_substep": 444.0 + 56.0 * iters, "achieved": pipeline_gbs,
                               "frac": pipeline_gbs / peak},
         **({"issue_roofline": issue} if issue else {}),
+        **({"stage_issue_rooflines": stage_issue} if stage_issue else {}),
         "particle_substeps_per_s": value / iters,
         "stage_replay": {"frames": args.steps, "bit_identical_to_timed_frames": stage_replay_identical,
                          "stage_sum_ms_per_step": stage_sum, "ratio_to_ms_per_step": stage_sum / frame_ms},
