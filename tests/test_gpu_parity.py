@@ -190,7 +190,7 @@ def test_tiny_coordinates_bit_exact(algorithm, pbf_mod, oracle_mod, cuda_device)
     that may hold such a friend (the 27 cells around it) divide the IEEE way
     for the rest of the substep.  A block at the origin (no clamp) with some
     particles moved onto tiny coordinates next to neighbours at exactly 0;
-    each friends build records the cells the taint kernel marks."""
+    each friends build marks the cells around them itself."""
     params, pos, vel = scene(pbf_mod, (10, 10, 10), origin=(0.0, 0.0, 0.0), jitter=0.0, boxClamp=0)
     pos[1, 0] = np.float32(3e-13)       # x next to particle 0 at x = 0
     pos[10, 1] = np.float32(1e-30)      # y, a normal float far below 2^-27
